@@ -1,0 +1,732 @@
+// api.cpp -- the C ABI (include/aloha.h): context, bricks, transfer function,
+// virtual ranks, views and the render entry points.
+//
+// The context replaces maui::Renderer (waikikiRenderer.cpp:344-1080) for the
+// volume path on one GPU: bricks are kept resident in HBM in a padded layout,
+// every camera change recomputes the per-view schedule (rank order and each
+// rank's front-to-back brick list), and render() launches one fused kernel.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "batch_internal.h"
+#include "internal.h"
+#include "order.h"
+
+using namespace aloha;
+
+namespace {
+
+struct ViewState {
+  bool has_camera = false, has_size = false, dirty = true;
+  float org[3], dir_00[3], dir_du[3], dir_dv[3];
+  int width = 0, height = 0;
+  Schedule sched;
+  float4* accum = nullptr;  // [n_ranks][H*W]
+  size_t accum_elems = 0;
+};
+
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t want) {
+    if (want <= bytes) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e == cudaSuccess) bytes = want;
+    return e;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+};
+
+bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+bool is_device_pointer(const void* p) {
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+struct aloha_ctx {
+  int device = 0;
+  int num_sms = 0;
+  std::string last_error;
+  // bricks
+  std::vector<aloha_brick_desc> descs;
+  std::vector<Box> boxes;
+  std::vector<DevBrick> dev_bricks;
+  std::vector<char> brick_present;
+  std::vector<size_t> brick_offset;  // float offset of each padded brick in `voxels`
+  DeviceBuffer voxels, bricks_dev, staging_in;
+  float bounds_lo[3] = {0, 0, 0}, bounds_hi[3] = {0, 0, 0};
+  // transfer function
+  DeviceBuffer tf;
+  int n_tf = 0;
+  // virtual ranks
+  int n_ranks = 0;
+  std::vector<int> brick_rank;
+  std::vector<KdNode> tree;
+  // views
+  std::vector<ViewState> views;
+  DeviceBuffer views_dev, sched_dev;
+  int sched_stride = 0;  // ints per view slot
+  // params, scratch
+  aloha_render_params params;
+  DeviceBuffer counter, flag, staging_out;
+  uint64_t last_samples = 0;
+  bool samples_valid = false;
+
+  int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    last_error = buf;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* what) {
+    return fail(ALOHA_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  }
+};
+
+#define CUDA_TRY(ctx, call)                                 \
+  do {                                                      \
+    cudaError_t _e = (call);                                \
+    if (_e != cudaSuccess) return (ctx)->cuda_fail(_e, #call); \
+  } while (0)
+
+namespace {
+
+// Upload dirty view state (camera, size, schedule) for `view` on `s`.
+int prepare_view(aloha_ctx* c, int view, cudaStream_t s) {
+  if (c->descs.empty()) return c->fail(ALOHA_ERR_NOT_READY, "no bricks uploaded");
+  if (c->n_tf == 0) return c->fail(ALOHA_ERR_NOT_READY, "no transfer function set");
+  if (view < 0 || view >= (int)c->views.size()) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "view %d has no state", view);
+  ViewState& v = c->views[view];
+  if (!v.has_camera) return c->fail(ALOHA_ERR_NOT_READY, "view %d has no camera", view);
+  if (!v.has_size) return c->fail(ALOHA_ERR_NOT_READY, "view %d has no size", view);
+  for (size_t b = 0; b < c->brick_present.size(); ++b)
+    if (!c->brick_present[b]) return c->fail(ALOHA_ERR_MISSING_BRICK, "brick %zu has no data (dropped)", b);
+  const int nb = (int)c->descs.size();
+  const int stride = 2 * c->n_ranks + 1 + nb;
+  if (stride != c->sched_stride) {
+    CUDA_TRY(c, c->sched_dev.ensure(sizeof(int) * (size_t)stride * kMaxViews));
+    c->sched_stride = stride;
+    for (auto& vv : c->views) vv.dirty = true;
+  }
+  if (!v.dirty) return ALOHA_OK;
+  v.sched = make_schedule(c->boxes, c->brick_rank, c->n_ranks, c->tree, c->params.order_mode, v.org);
+  // every rank appears exactly once in the composite order
+  std::vector<char> seen(c->n_ranks, 0);
+  std::vector<int> order;
+  for (int r : v.sched.rank_order)
+    if (r >= 0 && r < c->n_ranks && !seen[r]) {
+      seen[r] = 1;
+      order.push_back(r);
+    }
+  for (int r = 0; r < c->n_ranks; ++r)
+    if (!seen[r]) order.push_back(r);
+  v.sched.rank_order = order;
+  std::vector<int> slot;
+  slot.reserve(stride);
+  slot.insert(slot.end(), order.begin(), order.end());
+  slot.insert(slot.end(), v.sched.rank_start.begin(), v.sched.rank_start.end());
+  slot.insert(slot.end(), v.sched.rank_bricks.begin(), v.sched.rank_bricks.end());
+  slot.resize(stride, 0);
+  DevView dv{};
+  for (int a = 0; a < 3; ++a) {
+    dv.org[a] = v.org[a];
+    dv.dir_00[a] = v.dir_00[a];
+    dv.dir_du[a] = v.dir_du[a];
+    dv.dir_dv[a] = v.dir_dv[a];
+  }
+  dv.width = v.width;
+  dv.height = v.height;
+  // maxDepth as handleCameraEvent computes it (waikikiRenderer.cpp:858-859)
+  {
+    float ctr[3], s1 = 0.f, s2 = 0.f;
+    for (int a = 0; a < 3; ++a) ctr[a] = (c->bounds_lo[a] + c->bounds_hi[a]) / 2.f;
+    for (int a = 0; a < 3; ++a) {
+      const float q = ctr[a] + c->bounds_hi[a];
+      s1 = s1 + q * q;
+      const float o = v.org[a] + ctr[a];
+      s2 = s2 + o * o;
+    }
+    dv.max_depth = std::sqrt(s2) + std::sqrt(s1);
+  }
+  dv.n_ranks = c->n_ranks;
+  dv.sched = view * stride;
+  int* sched_dst = static_cast<int*>(c->sched_dev.ptr) + (size_t)view * stride;
+  CUDA_TRY(c, cudaMemcpyAsync(sched_dst, slot.data(), sizeof(int) * stride, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(c, cudaMemcpyAsync(static_cast<DevView*>(c->views_dev.ptr) + view, &dv, sizeof dv,
+                              cudaMemcpyHostToDevice, s));
+  v.dirty = false;
+  return ALOHA_OK;
+}
+
+// Per-view accumulation buffer when the parameters ask for it.
+int prepare_accum(aloha_ctx* c, int view, cudaStream_t s, float4** out) {
+  *out = nullptr;
+  const aloha_render_params& p = c->params;
+  if (!p.accumulate && p.accum_id == 0) return ALOHA_OK;
+  ViewState& v = c->views[view];
+  const size_t elems = (size_t)c->n_ranks * v.width * v.height;
+  if (v.accum_elems != elems) {
+    if (p.accum_id > 0)
+      return c->fail(ALOHA_ERR_NOT_READY, "accum_id > 0 but view %d has no accumulation buffer of this size", view);
+    if (v.accum) cudaFree(v.accum);
+    v.accum = nullptr;
+    v.accum_elems = 0;
+    CUDA_TRY(c, cudaMalloc(&v.accum, elems * sizeof(float4)));
+    CUDA_TRY(c, cudaMemsetAsync(v.accum, 0, elems * sizeof(float4), s));
+    v.accum_elems = elems;
+  }
+  *out = v.accum;
+  return ALOHA_OK;
+}
+
+FrameArgs frame_args(aloha_ctx* c) {
+  const aloha_render_params& p = c->params;
+  FrameArgs a{};
+  a.bricks = static_cast<const DevBrick*>(c->bricks_dev.ptr);
+  a.views = static_cast<const DevView*>(c->views_dev.ptr);
+  a.sched = static_cast<const int*>(c->sched_dev.ptr);
+  a.tf = static_cast<const float4*>(c->tf.ptr);
+  a.n_tf = c->n_tf;
+  a.dt = p.dt;
+  a.et_alpha = p.et_alpha;
+  a.jitter_mode = p.jitter_mode;
+  a.jitter_value = p.jitter_value;
+  a.crosshair = p.crosshair;
+  a.spp = p.spp;
+  a.accum_id = p.accum_id;
+  a.accumulate = p.accumulate;
+  a.heat_map = p.heat_map;
+  a.heat_map_scale = p.heat_map_scale;
+  a.composite_mode = p.composite_mode;
+  a.island_id = p.island_id;
+  a.num_islands = p.num_islands;
+  a.counter = static_cast<unsigned long long*>(c->counter.ptr);
+  return a;
+}
+
+int check_params(aloha_ctx* c, const aloha_render_params* p) {
+  if (!(std::isfinite(p->dt) && p->dt > 0.f)) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "dt must be finite and > 0");
+  if (!(std::isfinite(p->et_alpha) && p->et_alpha > 0.f))
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "et_alpha must be finite and > 0");
+  if (p->jitter_mode < 0 || p->jitter_mode > 2) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "bad jitter_mode");
+  if (!std::isfinite(p->jitter_value)) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "jitter_value must be finite");
+  if (p->spp < 1 || p->spp > 4096) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "spp must be in [1, 4096]");
+  if (p->accum_id < 0) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "accum_id must be >= 0");
+  if (p->composite_mode != ALOHA_COMPOSITE_FP32 && p->composite_mode != ALOHA_COMPOSITE_UBYTE)
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "bad composite_mode");
+  if (p->order_mode != ALOHA_ORDER_FACES && p->order_mode != ALOHA_ORDER_REFERENCE_KD)
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "bad order_mode");
+  if (p->num_islands < 1 || p->island_id < 0 || p->island_id >= p->num_islands)
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "need num_islands >= 1 and 0 <= island_id < num_islands");
+  if (!std::isfinite(p->heat_map_scale)) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "heat_map_scale not finite");
+  return ALOHA_OK;
+}
+
+int set_partition(aloha_ctx* c, int n_ranks) {
+  std::vector<int> br;
+  std::vector<KdNode> tree;
+  if (!partition_kd(c->boxes, n_ranks, br, tree))
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "partitionKD made no progress for %d ranks", n_ranks);
+  c->n_ranks = n_ranks;
+  c->brick_rank = br;
+  c->tree = tree;
+  for (auto& v : c->views) v.dirty = true;
+  return ALOHA_OK;
+}
+
+// Copies host output bytes back after the stream finished.
+int finish_host_output(aloha_ctx* c, void* host_dst, const void* dev_src, size_t bytes, cudaStream_t s) {
+  CUDA_TRY(c, cudaMemcpyAsync(host_dst, dev_src, bytes, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(c, cudaStreamSynchronize(s));
+  return ALOHA_OK;
+}
+
+}  // namespace
+
+namespace aloha {
+
+int ctx_fail(aloha_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  c->last_error = buf;
+  return code;
+}
+int ctx_device(const aloha_ctx* c) { return c->device; }
+int ctx_num_sms(const aloha_ctx* c) { return c->num_sms; }
+int ctx_n_tf(const aloha_ctx* c) { return c->n_tf; }
+void ctx_view_size(const aloha_ctx* c, int view, int* w, int* h) {
+  *w = c->views[view].width;
+  *h = c->views[view].height;
+}
+void ctx_frame_args(aloha_ctx* c, FrameArgs* a) { *a = frame_args(c); }
+int ctx_prepare_view(aloha_ctx* c, int view, cudaStream_t s) { return prepare_view(c, view, s); }
+void ctx_mark_samples(aloha_ctx* c) { c->samples_valid = true; }
+bool ctx_is_device_pointer(const void* p) { return is_device_pointer(p); }
+
+}  // namespace aloha
+
+extern "C" {
+
+int aloha_abi_version(void) { return ALOHA_ABI_VERSION; }
+
+const char* aloha_status_string(int status) {
+  switch (status) {
+    case ALOHA_OK: return "ok";
+    case ALOHA_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case ALOHA_ERR_NULL_POINTER: return "null pointer";
+    case ALOHA_ERR_OUT_OF_RANGE: return "index out of range";
+    case ALOHA_ERR_NOT_READY: return "not ready";
+    case ALOHA_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case ALOHA_ERR_CUDA: return "CUDA error";
+    case ALOHA_ERR_TIMEOUT: return "device wait timed out";
+    case ALOHA_ERR_MISSING_BRICK: return "missing brick";
+    case ALOHA_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+int aloha_default_render_params(aloha_render_params* out) {
+  if (!out) return ALOHA_ERR_NULL_POINTER;
+  std::memset(out, 0, sizeof *out);
+  out->dt = 0.5f;
+  out->et_alpha = 0.99f;
+  out->jitter_mode = ALOHA_JITTER_HASH;
+  out->jitter_value = 0.f;
+  out->crosshair = 0;
+  out->spp = 1;
+  out->accum_id = 0;
+  out->accumulate = 0;
+  out->heat_map = 0;
+  out->heat_map_scale = 1e-5f;
+  out->composite_mode = ALOHA_COMPOSITE_FP32;
+  out->island_id = 0;
+  out->num_islands = 1;
+  out->order_mode = ALOHA_ORDER_FACES;
+  return ALOHA_OK;
+}
+
+int aloha_create(int device, aloha_ctx** out) {
+  if (!out) return ALOHA_ERR_NULL_POINTER;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return ALOHA_ERR_CUDA;
+  }
+  if (device < 0 || device >= count) return ALOHA_ERR_OUT_OF_RANGE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return ALOHA_ERR_CUDA;
+  // kernels are built for sm_103a only
+  if (prop.major != 10 || prop.minor != 3) return ALOHA_ERR_UNSUPPORTED;
+  if (cudaSetDevice(device) != cudaSuccess) return ALOHA_ERR_CUDA;
+  aloha_ctx* c = new (std::nothrow) aloha_ctx();
+  if (!c) return ALOHA_ERR_OUT_OF_MEMORY;
+  c->device = device;
+  c->num_sms = prop.multiProcessorCount;
+  aloha_default_render_params(&c->params);
+  if (c->views_dev.ensure(sizeof(DevView) * kMaxViews) != cudaSuccess ||
+      c->counter.ensure(sizeof(unsigned long long)) != cudaSuccess || c->flag.ensure(sizeof(int)) != cudaSuccess) {
+    delete c;
+    return ALOHA_ERR_OUT_OF_MEMORY;
+  }
+  *out = c;
+  return ALOHA_OK;
+}
+
+int aloha_destroy(aloha_ctx* c) {
+  if (!c) return ALOHA_ERR_NULL_POINTER;
+  cudaSetDevice(c->device);
+  cudaDeviceSynchronize();
+  for (auto& v : c->views)
+    if (v.accum) cudaFree(v.accum);
+  for (DeviceBuffer* b : {&c->voxels, &c->bricks_dev, &c->staging_in, &c->tf, &c->views_dev, &c->sched_dev,
+                          &c->counter, &c->flag, &c->staging_out})
+    b->release();
+  delete c;
+  return ALOHA_OK;
+}
+
+const char* aloha_last_error(const aloha_ctx* c) { return c ? c->last_error.c_str() : "null context"; }
+
+int aloha_set_render_params(aloha_ctx* c, const aloha_render_params* p) {
+  if (!c || !p) return ALOHA_ERR_NULL_POINTER;
+  int rc = check_params(c, p);
+  if (rc) return rc;
+  if (p->order_mode != c->params.order_mode)
+    for (auto& v : c->views) v.dirty = true;
+  c->params = *p;
+  return ALOHA_OK;
+}
+
+// Uploads one brick's voxels into its padded slot.
+static int upload_brick(aloha_ctx* c, int b, const float* src) {
+  const aloha_brick_desc& d = c->descs[b];
+  const int nx = d.voxel_hi[0] - d.voxel_lo[0], ny = d.voxel_hi[1] - d.voxel_lo[1], nz = d.voxel_hi[2] - d.voxel_lo[2];
+  const size_t raw = (size_t)nx * ny * nz;
+  const float* dsrc = src;
+  if (!is_device_pointer(src)) {
+    CUDA_TRY(c, c->staging_in.ensure(raw * sizeof(float)));
+    CUDA_TRY(c, cudaMemcpy(c->staging_in.ptr, src, raw * sizeof(float), cudaMemcpyHostToDevice));
+    dsrc = static_cast<const float*>(c->staging_in.ptr);
+  }
+  const DevBrick& db = c->dev_bricks[b];
+  float* alloc = static_cast<float*>(c->voxels.ptr) + c->brick_offset[b];
+  CUDA_TRY(c, cudaMemset(c->flag.ptr, 0, sizeof(int)));
+  CUDA_TRY(c, launch_pad_brick(dsrc, nx, ny, nz, alloc, db.sy, db.sz / db.sy, nz + 2 * kApron,
+                               static_cast<int*>(c->flag.ptr), 0));
+  int bad = 0;
+  CUDA_TRY(c, cudaMemcpy(&bad, c->flag.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (bad) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "brick %d holds a non-finite voxel", b);
+  c->brick_present[b] = 1;
+  return ALOHA_OK;
+}
+
+int aloha_set_bricks(aloha_ctx* c, const aloha_brick_desc* descs, const float* const* voxels, int n) {
+  if (!c || !descs || !voxels) return ALOHA_ERR_NULL_POINTER;
+  if (n <= 0 || n > 65536) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "brick count %d not in [1, 65536]", n);
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  size_t total = 0;
+  std::vector<size_t> offs(n);
+  std::vector<DevBrick> db(n);
+  for (int b = 0; b < n; ++b) {
+    const aloha_brick_desc& d = descs[b];
+    if (!voxels[b]) return c->fail(ALOHA_ERR_NULL_POINTER, "voxels[%d] is null", b);
+    int nsz[3];
+    for (int a = 0; a < 3; ++a) {
+      nsz[a] = d.voxel_hi[a] - d.voxel_lo[a];
+      if (nsz[a] <= 0 || nsz[a] > 16384)
+        return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "brick %d: voxel range size %d on axis %d", b, nsz[a], a);
+      if (!(std::isfinite(d.space_lo[a]) && std::isfinite(d.space_hi[a]) && d.space_lo[a] < d.space_hi[a]))
+        return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "brick %d: empty or non-finite space range", b);
+    }
+    // rows padded to a multiple of 8 floats (32-byte aligned rows)
+    const int px = ((nsz[0] + 2 * kApron) + 7) & ~7, py = nsz[1] + 2 * kApron, pz = nsz[2] + 2 * kApron;
+    const size_t elems = (size_t)px * py * pz;
+    if (elems >= (size_t)1 << 31)
+      return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "brick %d too large for 32-bit voxel offsets; split it", b);
+    offs[b] = total;
+    total += (elems + 63) & ~(size_t)63;  // 256-byte aligned bricks
+    db[b].sy = px;
+    db[b].sz = px * py;
+    for (int a = 0; a < 3; ++a) {
+      db[b].n[a] = nsz[a];
+      db[b].lo[a] = (float)d.voxel_lo[a];
+      db[b].space_lo[a] = d.space_lo[a];
+      db[b].space_hi[a] = d.space_hi[a];
+    }
+  }
+  size_t free_b = 0, total_b = 0;
+  CUDA_TRY(c, cudaMemGetInfo(&free_b, &total_b));
+  if (total * sizeof(float) > free_b + c->voxels.bytes)
+    return c->fail(ALOHA_ERR_OUT_OF_MEMORY, "bricks need %zu bytes, %zu free", total * sizeof(float), free_b);
+  CUDA_TRY(c, cudaDeviceSynchronize());
+  CUDA_TRY(c, c->voxels.ensure(total * sizeof(float)));
+  for (int b = 0; b < n; ++b)
+    db[b].base = static_cast<const float*>(c->voxels.ptr) + offs[b] + (size_t)kApron * db[b].sz +
+                 (size_t)kApron * db[b].sy + kApron;
+  c->descs.assign(descs, descs + n);
+  c->dev_bricks = db;
+  c->brick_offset = offs;
+  c->brick_present.assign(n, 0);
+  c->boxes.resize(n);
+  for (int a = 0; a < 3; ++a) {
+    c->bounds_lo[a] = 1e30f;
+    c->bounds_hi[a] = -1e30f;
+  }
+  for (int b = 0; b < n; ++b)
+    for (int a = 0; a < 3; ++a) {
+      c->boxes[b].lo[a] = descs[b].space_lo[a];
+      c->boxes[b].hi[a] = descs[b].space_hi[a];
+      c->bounds_lo[a] = std::min(c->bounds_lo[a], descs[b].space_lo[a]);
+      c->bounds_hi[a] = std::max(c->bounds_hi[a], descs[b].space_hi[a]);
+    }
+  CUDA_TRY(c, c->bricks_dev.ensure(sizeof(DevBrick) * n));
+  CUDA_TRY(c, cudaMemcpy(c->bricks_dev.ptr, db.data(), sizeof(DevBrick) * n, cudaMemcpyHostToDevice));
+  for (int b = 0; b < n; ++b) {
+    int rc = upload_brick(c, b, voxels[b]);
+    if (rc) {
+      c->descs.clear();
+      return rc;
+    }
+  }
+  c->staging_in.release();
+  c->sched_stride = 0;
+  return set_partition(c, n);
+}
+
+int aloha_update_brick(aloha_ctx* c, int brick, const float* voxels) {
+  if (!c || !voxels) return ALOHA_ERR_NULL_POINTER;
+  if (brick < 0 || brick >= (int)c->descs.size()) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "brick %d", brick);
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  CUDA_TRY(c, cudaDeviceSynchronize());
+  return upload_brick(c, brick, voxels);
+}
+
+int aloha_drop_brick(aloha_ctx* c, int brick) {
+  if (!c) return ALOHA_ERR_NULL_POINTER;
+  if (brick < 0 || brick >= (int)c->descs.size()) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "brick %d", brick);
+  c->brick_present[brick] = 0;
+  return ALOHA_OK;
+}
+
+int aloha_set_transfer_function(aloha_ctx* c, const float* rgba, int n) {
+  if (!c || !rgba) return ALOHA_ERR_NULL_POINTER;
+  if (n < 1 || n > kMaxTF) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "transfer function size %d not in [1, %d]", n, kMaxTF);
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  std::vector<float> h((size_t)n * 4);
+  if (is_device_pointer(rgba))
+    CUDA_TRY(c, cudaMemcpy(h.data(), rgba, h.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  else
+    std::memcpy(h.data(), rgba, h.size() * sizeof(float));
+  for (float v : h)
+    if (!std::isfinite(v)) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "transfer function holds a non-finite value");
+  CUDA_TRY(c, cudaDeviceSynchronize());
+  CUDA_TRY(c, c->tf.ensure(h.size() * sizeof(float)));
+  CUDA_TRY(c, cudaMemcpy(c->tf.ptr, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+  c->n_tf = n;
+  return ALOHA_OK;
+}
+
+int aloha_set_ranks(aloha_ctx* c, int n_ranks) {
+  if (!c) return ALOHA_ERR_NULL_POINTER;
+  if (c->descs.empty()) return c->fail(ALOHA_ERR_NOT_READY, "no bricks uploaded");
+  if (n_ranks < 1 || n_ranks > (int)c->descs.size())
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "n_ranks %d not in [1, %zu]", n_ranks, c->descs.size());
+  return set_partition(c, n_ranks);
+}
+
+int aloha_set_rank_assignment(aloha_ctx* c, const int* brick_rank, int n_bricks, int n_ranks) {
+  if (!c || !brick_rank) return ALOHA_ERR_NULL_POINTER;
+  if (n_bricks != (int)c->descs.size())
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "assignment covers %d bricks, context has %zu", n_bricks, c->descs.size());
+  if (n_ranks < 1 || n_ranks > n_bricks) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "bad n_ranks %d", n_ranks);
+  for (int b = 0; b < n_bricks; ++b)
+    if (brick_rank[b] < 0 || brick_rank[b] >= n_ranks)
+      return c->fail(ALOHA_ERR_MISSING_BRICK, "brick %d is assigned to no rank", b);
+  c->n_ranks = n_ranks;
+  c->brick_rank.assign(brick_rank, brick_rank + n_bricks);
+  c->tree.clear();
+  for (auto& v : c->views) v.dirty = true;
+  return ALOHA_OK;
+}
+
+int aloha_set_camera(aloha_ctx* c, int view, const float* org, const float* dir_00, const float* dir_du,
+                     const float* dir_dv) {
+  if (!c || !org || !dir_00 || !dir_du || !dir_dv) return ALOHA_ERR_NULL_POINTER;
+  if (view < 0 || view >= kMaxViews) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "view %d not in [0, %d)", view, kMaxViews);
+  if (!finite3(org) || !finite3(dir_00) || !finite3(dir_du) || !finite3(dir_dv))
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "camera holds a non-finite value");
+  if ((int)c->views.size() <= view) c->views.resize(view + 1);
+  ViewState& v = c->views[view];
+  std::memcpy(v.org, org, 12);
+  std::memcpy(v.dir_00, dir_00, 12);
+  std::memcpy(v.dir_du, dir_du, 12);
+  std::memcpy(v.dir_dv, dir_dv, 12);
+  v.has_camera = true;
+  v.dirty = true;
+  return ALOHA_OK;
+}
+
+int aloha_resize(aloha_ctx* c, int view, int width, int height) {
+  if (!c) return ALOHA_ERR_NULL_POINTER;
+  if (view < 0 || view >= kMaxViews) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "view %d not in [0, %d)", view, kMaxViews);
+  if (width < 1 || height < 1 || width > 32768 || height > 32768 || (long long)width * height > (1ll << 30))
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "frame size %dx%d out of range", width, height);
+  if ((int)c->views.size() <= view) c->views.resize(view + 1);
+  ViewState& v = c->views[view];
+  if (v.width != width || v.height != height) {
+    if (v.accum) cudaFree(v.accum);
+    v.accum = nullptr;
+    v.accum_elems = 0;
+  }
+  v.width = width;
+  v.height = height;
+  v.has_size = true;
+  v.dirty = true;
+  return ALOHA_OK;
+}
+
+int aloha_get_composite_order(aloha_ctx* c, int view, int* rank_order, int max_ranks, int* n_ranks) {
+  if (!c || !rank_order || !n_ranks) return ALOHA_ERR_NULL_POINTER;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  int rc = prepare_view(c, view, 0);
+  if (rc) return rc;
+  CUDA_TRY(c, cudaStreamSynchronize(0));
+  const std::vector<int>& o = c->views[view].sched.rank_order;
+  if ((int)o.size() > max_ranks) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "order needs %zu entries", o.size());
+  std::copy(o.begin(), o.end(), rank_order);
+  *n_ranks = (int)o.size();
+  return ALOHA_OK;
+}
+
+int aloha_render(aloha_ctx* c, int view, uint32_t* fb, void* stream) {
+  if (!c || !fb) return ALOHA_ERR_NULL_POINTER;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  int rc = prepare_view(c, view, s);
+  if (rc) return rc;
+  const ViewState& v = c->views[view];
+  FrameArgs a = frame_args(c);
+  rc = prepare_accum(c, view, s, &a.accum);
+  if (rc) return rc;
+  const size_t npx = (size_t)v.width * v.height;
+  const bool host = !is_device_pointer(fb);
+  if (host) {
+    CUDA_TRY(c, c->staging_out.ensure(npx * sizeof(uint32_t)));
+    a.fb = static_cast<uint32_t*>(c->staging_out.ptr);
+  } else {
+    a.fb = fb;
+  }
+  CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
+  CUDA_TRY(c, launch_render(a, view, v.width, v.height, s));
+  c->samples_valid = true;
+  if (host) return finish_host_output(c, fb, a.fb, npx * sizeof(uint32_t), s);
+  return ALOHA_OK;
+}
+
+int aloha_render_partials(aloha_ctx* c, int view, float* rank_images, float* rank_depth, void* stream) {
+  if (!c || !rank_images) return ALOHA_ERR_NULL_POINTER;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  int rc = prepare_view(c, view, s);
+  if (rc) return rc;
+  const ViewState& v = c->views[view];
+  FrameArgs a = frame_args(c);
+  rc = prepare_accum(c, view, s, &a.accum);
+  if (rc) return rc;
+  const size_t npx = (size_t)v.width * v.height;
+  const size_t img_bytes = (size_t)c->n_ranks * npx * sizeof(float4);
+  const size_t depth_bytes = rank_depth ? (size_t)c->n_ranks * npx * sizeof(float) : 0;
+  const bool host_img = !is_device_pointer(rank_images);
+  const bool host_depth = rank_depth && !is_device_pointer(rank_depth);
+  if (host_img || host_depth) CUDA_TRY(c, c->staging_out.ensure(img_bytes + depth_bytes));
+  char* stage = static_cast<char*>(c->staging_out.ptr);
+  a.rank_images = host_img ? reinterpret_cast<float4*>(stage) : reinterpret_cast<float4*>(rank_images);
+  a.rank_depth = rank_depth ? (host_depth ? reinterpret_cast<float*>(stage + img_bytes) : rank_depth) : nullptr;
+  a.fb = nullptr;
+  CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
+  CUDA_TRY(c, launch_render(a, view, v.width, v.height, s));
+  c->samples_valid = true;
+  if (host_img) CUDA_TRY(c, cudaMemcpyAsync(rank_images, a.rank_images, img_bytes, cudaMemcpyDeviceToHost, s));
+  if (host_depth) CUDA_TRY(c, cudaMemcpyAsync(rank_depth, a.rank_depth, depth_bytes, cudaMemcpyDeviceToHost, s));
+  if (host_img || host_depth) CUDA_TRY(c, cudaStreamSynchronize(s));
+  return ALOHA_OK;
+}
+
+int aloha_get_stats(aloha_ctx* c, aloha_stats* out) {
+  if (!c || !out) return ALOHA_ERR_NULL_POINTER;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  std::memset(out, 0, sizeof *out);
+  if (c->samples_valid) {
+    unsigned long long n = 0;
+    CUDA_TRY(c, cudaMemcpy(&n, c->counter.ptr, sizeof n, cudaMemcpyDeviceToHost));
+    out->samples = n;
+  }
+  out->n_bricks = (int)c->descs.size();
+  out->n_ranks = c->n_ranks;
+  out->brick_bytes = c->voxels.bytes;
+  return ALOHA_OK;
+}
+
+// ------------------------------------------------------------ composite
+
+static int composite_common(const void* imgs, size_t img_bytes, const int* order, int n_ranks, int width, int height,
+                            int mode, uint32_t* fb, void* stream, bool u8) {
+  if (!imgs || !order || !fb) return ALOHA_ERR_NULL_POINTER;
+  if (n_ranks < 1 || width < 1 || height < 1 || (long long)width * height > (1ll << 30))
+    return ALOHA_ERR_INVALID_ARGUMENT;
+  if (mode != ALOHA_COMPOSITE_FP32 && mode != ALOHA_COMPOSITE_UBYTE) return ALOHA_ERR_INVALID_ARGUMENT;
+  std::vector<int> h_order(n_ranks);
+  if (is_device_pointer(order)) {
+    if (cudaMemcpy(h_order.data(), order, sizeof(int) * n_ranks, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return ALOHA_ERR_CUDA;
+  } else {
+    std::memcpy(h_order.data(), order, sizeof(int) * n_ranks);
+  }
+  for (int r : h_order)
+    if (r < 0 || r >= n_ranks) return ALOHA_ERR_OUT_OF_RANGE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t npx = (size_t)width * height;
+  const bool host_in = !is_device_pointer(imgs), host_out = !is_device_pointer(fb);
+  void* d_in = nullptr;
+  uint32_t* d_out = nullptr;
+  int* d_order = nullptr;
+  int rc = ALOHA_OK;
+  auto fail = [&](int code) {
+    rc = code;
+    return code;
+  };
+  do {
+    if (cudaMalloc(&d_order, sizeof(int) * n_ranks) != cudaSuccess) { fail(ALOHA_ERR_OUT_OF_MEMORY); break; }
+    if (cudaMemcpyAsync(d_order, h_order.data(), sizeof(int) * n_ranks, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+      fail(ALOHA_ERR_CUDA);
+      break;
+    }
+    const void* in = imgs;
+    if (host_in) {
+      if (cudaMalloc(&d_in, img_bytes) != cudaSuccess) { fail(ALOHA_ERR_OUT_OF_MEMORY); break; }
+      if (cudaMemcpyAsync(d_in, imgs, img_bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) { fail(ALOHA_ERR_CUDA); break; }
+      in = d_in;
+    }
+    uint32_t* out = fb;
+    if (host_out) {
+      if (cudaMalloc(&d_out, npx * sizeof(uint32_t)) != cudaSuccess) { fail(ALOHA_ERR_OUT_OF_MEMORY); break; }
+      out = d_out;
+    }
+    cudaError_t e = u8 ? launch_composite_u8(static_cast<const uint32_t*>(in), d_order, n_ranks, (int)npx, out, s)
+                       : launch_composite_f32(static_cast<const float4*>(in), d_order, n_ranks, (int)npx, mode, out, s);
+    if (e != cudaSuccess) { fail(ALOHA_ERR_CUDA); break; }
+    if (host_out && cudaMemcpyAsync(fb, out, npx * sizeof(uint32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess) {
+      fail(ALOHA_ERR_CUDA);
+      break;
+    }
+  } while (0);
+  // temporaries: wait for the stream before freeing them
+  if (cudaStreamSynchronize(s) != cudaSuccess && rc == ALOHA_OK) rc = ALOHA_ERR_CUDA;
+  if (d_in) cudaFree(d_in);
+  if (d_out) cudaFree(d_out);
+  if (d_order) cudaFree(d_order);
+  return rc;
+}
+
+int aloha_composite_over(const float* rank_images, const int* order, int n_ranks, int width, int height, int mode,
+                         uint32_t* fb, void* stream) {
+  const size_t bytes = (size_t)n_ranks * width * height * sizeof(float4);
+  return composite_common(rank_images, bytes, order, n_ranks, width, height, mode, fb, stream, false);
+}
+
+int aloha_composite_over_rgba8(const uint32_t* rank_fbs, const int* order, int n_ranks, int width, int height,
+                               uint32_t* fb, void* stream) {
+  const size_t bytes = (size_t)n_ranks * width * height * sizeof(uint32_t);
+  return composite_common(rank_fbs, bytes, order, n_ranks, width, height, ALOHA_COMPOSITE_UBYTE, fb, stream, true);
+}
+
+}  // extern "C"

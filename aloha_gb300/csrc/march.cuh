@@ -1,0 +1,366 @@
+// march.cuh -- device functions of the volume march (sm_103a).
+//
+// Restates the reference's per-pixel path (deviceCode.cpp:94-107 ray
+// generation, 41-57 slab test, 245-254 firstSampleT, 256-298 integrateBrick,
+// 354-416 output stage).  This file is compiled with -fmad=false: every fused
+// multiply-add is an explicit fmaf, so the results are bit-identical to the
+// CPU restatement, which fixes the same evaluation order.
+//
+// Sampling: voxel-unit coordinate u = o + t*d - voxelRange.lower; the value
+// tap is the trilinear interpolation at u, the six gradient taps sit at
+// u +- 1/2 (the reference's tc +- 0.5/N, deviceCode.cpp:278-284).  u - 1/2 and
+// u + 1/2 differ by exactly 1, so all seven taps read one 20-voxel cross
+// around the cell and share their fractional weights: 20 loads per sample
+// instead of 56.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "internal.h"
+
+namespace aloha {
+
+__device__ __forceinline__ float lerpf(float a, float b, float w) { return fmaf(w, b - a, a); }
+
+__device__ __forceinline__ uint32_t pcg_hash(uint32_t v) {
+  uint32_t state = v * 747796405u + 2891336453u;
+  uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+  return (word >> 22u) ^ word;
+}
+
+// Per-brick ray offset ils_t0 (deviceCode.cpp:386) from (pixel, accumID, draw).
+__device__ __forceinline__ float jitter(int mode, float value, uint32_t pixel, uint32_t accum_id, uint32_t draw) {
+  if (mode == ALOHA_JITTER_CONST) return value;
+  if (mode == ALOHA_JITTER_HASH) {
+    uint32_t h = pcg_hash(pixel ^ pcg_hash(accum_id ^ pcg_hash(draw)));
+    return (float)(h >> 8) * (1.0f / 16777216.0f);
+  }
+  return 0.0f;
+}
+
+struct Ray {
+  float o[3], d[3];
+};
+
+// generateRay (deviceCode.cpp:94-107).
+__device__ __forceinline__ Ray generate_ray(const DevView& v, int x, int y) {
+  Ray r;
+  const float su = (float)x + 0.5f, sv = (float)y + 0.5f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    r.o[a] = v.org[a];
+    r.d[a] = fmaf(sv, v.dir_dv[a], fmaf(su, v.dir_du[a], v.dir_00[a]));
+  }
+  const float len2 = fmaf(r.d[2], r.d[2], fmaf(r.d[1], r.d[1], r.d[0] * r.d[0]));
+  const float inv = 1.0f / sqrtf(len2);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    r.d[a] = r.d[a] * inv;
+    if (fabsf(r.d[a]) < 1e-5f) r.d[a] = 1e-5f;
+  }
+  return r;
+}
+
+// Slab test (deviceCode.cpp:41-57) against a brick's space range.
+__device__ __forceinline__ bool slab(const Ray& r, const float lo[3], const float hi[3], float tmin, float tmax,
+                                     float& t0, float& t1) {
+  float nr[3], fr[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float l = (lo[a] - r.o[a]) / r.d[a];
+    const float h = (hi[a] - r.o[a]) / r.d[a];
+    nr[a] = fminf(l, h);
+    fr[a] = fmaxf(l, h);
+  }
+  t0 = fmaxf(tmin, fmaxf(fmaxf(nr[0], nr[1]), nr[2]));
+  t1 = fminf(tmax, fminf(fminf(fr[0], fr[1]), fr[2]));
+  return t0 < t1;
+}
+
+// firstSampleT (deviceCode.cpp:245-254).
+__device__ __forceinline__ float first_sample_t(float lower, float dt, float ils) {
+  const float n = floorf((lower - dt * ils) / dt);
+  float t = dt * (ils + n);
+  if (t < lower) t = t + dt;
+  return t;
+}
+
+// Seven-tap stencil at voxel coordinate (ux, uy, uz) of a padded brick.
+// Evaluation order (shared with the CPU restatement): taps displaced along an
+// axis interpolate bilinearly across that axis first (x: y then z; y: x then
+// z; z: x then y), then lerp along it; the value tap lerps the x-tap columns
+// along x.  lerp(a, b, w) = fmaf(w, b - a, a).
+struct StencilOut {
+  float value, gx, gy, gz;
+};
+
+__device__ __forceinline__ StencilOut stencil(const float* __restrict__ base, int sy, int sz, int nx, int ny, int nz,
+                                              float ux, float uy, float uz) {
+  const float mx = ux - 0.5f, my = uy - 0.5f, mz = uz - 0.5f;
+  const float fmx = floorf(mx), fmy = floorf(my), fmz = floorf(mz);
+  const float fcx = floorf(ux), fcy = floorf(uy), fcz = floorf(uz);
+  const float fx = mx - fmx, fy = my - fmy, fz = mz - fmz;  // weights of the displaced taps
+  const float gx = ux - fcx, gy = uy - fcy, gz = uz - fcz;  // weights of the centre
+  const bool hx = fcx != fmx, hy = fcy != fmy, hz = fcz != fmz;  // floor(u) == floor(u - 1/2) + 1
+  // Indices, clamped into the apron.  Every index the oracle clamps to the
+  // edge maps to an apron voxel holding that edge value, so these clamps only
+  // keep pathological coordinates in bounds and never change a value.
+  const int ix = min(max((int)fmx, -kApron), nx - 1);
+  const int iy = min(max((int)fmy, -kApron), ny - 1);
+  const int iz = min(max((int)fmz, -kApron), nz - 1);
+  const int cx = min(max((int)fcx, -kApron), nx);
+  const int cy = min(max((int)fcy, -kApron), ny);
+  const int cz = min(max((int)fcz, -kApron), nz);
+
+  // X region: x in {ix, ix+1, ix+2}, y in {cy, cy+1}, z in {cz, cz+1}.
+  const float* p0 = base + (cz * sz + cy * sy + ix);
+  const float a000 = __ldg(p0), a100 = __ldg(p0 + 1), a200 = __ldg(p0 + 2);
+  const float a010 = __ldg(p0 + sy), a110 = __ldg(p0 + sy + 1), a210 = __ldg(p0 + sy + 2);
+  const float a001 = __ldg(p0 + sz), a101 = __ldg(p0 + sz + 1), a201 = __ldg(p0 + sz + 2);
+  const float a011 = __ldg(p0 + sz + sy), a111 = __ldg(p0 + sz + sy + 1), a211 = __ldg(p0 + sz + sy + 2);
+  // Extra y row (iy or iy+2) and extra z slice (iz or iz+2) at x in {cx, cx+1}.
+  const int ye = hy ? iy : iy + 2;
+  const int ze = hz ? iz : iz + 2;
+  const float* p1 = base + (cz * sz + ye * sy + cx);
+  const float b00 = __ldg(p1), b10 = __ldg(p1 + 1), b01 = __ldg(p1 + sz), b11 = __ldg(p1 + sz + 1);
+  const float* p2 = base + (ze * sz + cy * sy + cx);
+  const float c00 = __ldg(p2), c10 = __ldg(p2 + 1), c01 = __ldg(p2 + sy), c11 = __ldg(p2 + sy + 1);
+
+  // x taps: columns X_k = bilinear (y by gy, then z by gz) at x = ix + k.
+  const float X0 = lerpf(lerpf(a000, a010, gy), lerpf(a001, a011, gy), gz);
+  const float X1 = lerpf(lerpf(a100, a110, gy), lerpf(a101, a111, gy), gz);
+  const float X2 = lerpf(lerpf(a200, a210, gy), lerpf(a201, a211, gy), gz);
+  StencilOut s;
+  s.value = lerpf(hx ? X1 : X0, hx ? X2 : X1, gx);
+  s.gx = lerpf(X1, X2, fx) - lerpf(X0, X1, fx);
+
+  // Voxels at x = cx, cx+1 of the four (y, z) rows of the X region.
+  const float v000 = hx ? a100 : a000, v100 = hx ? a200 : a100;
+  const float v010 = hx ? a110 : a010, v110 = hx ? a210 : a110;
+  const float v001 = hx ? a101 : a001, v101 = hx ? a201 : a101;
+  const float v011 = hx ? a111 : a011, v111 = hx ? a211 : a111;
+  // x lerps shared by the y and z taps
+  const float L00 = lerpf(v000, v100, gx);  // (cy,   cz)
+  const float L10 = lerpf(v010, v110, gx);  // (cy+1, cz)
+  const float L01 = lerpf(v001, v101, gx);  // (cy,   cz+1)
+  const float L11 = lerpf(v011, v111, gx);  // (cy+1, cz+1)
+
+  // y taps: rows bilinear (x by gx, then z by gz).
+  const float Yc0 = lerpf(L00, L01, gz);
+  const float Yc1 = lerpf(L10, L11, gz);
+  const float Ye = lerpf(lerpf(b00, b10, gx), lerpf(b01, b11, gx), gz);
+  const float Y0 = hy ? Ye : Yc0, Y1 = hy ? Yc0 : Yc1, Y2 = hy ? Yc1 : Ye;
+  s.gy = lerpf(Y1, Y2, fy) - lerpf(Y0, Y1, fy);
+
+  // z taps: slices bilinear (x by gx, then y by gy).
+  const float Zc0 = lerpf(L00, L10, gy);
+  const float Zc1 = lerpf(L01, L11, gy);
+  const float Ze = lerpf(lerpf(c00, c10, gx), lerpf(c01, c11, gx), gy);
+  const float Z0 = hz ? Ze : Zc0, Z1 = hz ? Zc0 : Zc1, Z2 = hz ? Zc1 : Ze;
+  s.gz = lerpf(Z1, Z2, fz) - lerpf(Z0, Z1, fz);
+  return s;
+}
+
+// tex1D on the transfer function (linear, normalized coords, border 0;
+// waikikiRenderer.cpp:990-1008).  tf_s holds the n entries at [2, n+2) with
+// two zero entries on each side.
+__device__ __forceinline__ float4 tf_lookup(const float4* __restrict__ tf_s, int n, float nf, float v) {
+  const float xb = v * nf - 0.5f;
+  const float fl = floorf(xb);
+  const float w = xb - fl;
+  const int i = min(max((int)fl, -2), n);
+  const float4 e0 = tf_s[i + 2];
+  const float4 e1 = tf_s[i + 3];
+  return make_float4(lerpf(e0.x, e1.x, w), lerpf(e0.y, e1.y, w), lerpf(e0.z, e1.z, w), lerpf(e0.w, e1.w, w));
+}
+
+// Iteration cap of one brick march: twice the lattice points in [t0, t1) plus
+// 16.  It never binds while t advances by about dt; it ends the loop when
+// t + dt rounds back to t (ray parameters beyond ~2^24 dt).
+__device__ __forceinline__ uint32_t march_cap(float t0, float t1, float dt) {
+  const float span = (t1 - t0) / dt;
+  return span < 1e8f ? (uint32_t)(span * 2.0f) + 16u : 200000016u;
+}
+
+// integrateBrick (deviceCode.cpp:256-298) over [t0, t1); returns the number
+// of samples taken.
+__device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
+                                                const Ray& r, float t0, float t1, float ils, float dt, float et,
+                                                float4& color) {
+  const float* __restrict__ base = b.base;
+  const int sy = b.sy, sz = b.sz, nx = b.n[0], ny = b.n[1], nz = b.n[2];
+  const float lox = b.lo[0], loy = b.lo[1], loz = b.lo[2];
+  const float nf = (float)n_tf;
+  const uint32_t cap = march_cap(t0, t1, dt);
+  uint32_t n = 0;
+  for (float t = first_sample_t(t0, dt, ils); t < t1 && color.w < et && n < cap; t = t + dt) {
+    ++n;
+    const float ux = fmaf(t, r.d[0], r.o[0]) - lox;
+    const float uy = fmaf(t, r.d[1], r.o[1]) - loy;
+    const float uz = fmaf(t, r.d[2], r.o[2]) - loz;
+    const StencilOut s = stencil(base, sy, sz, nx, ny, nz, ux, uy, uz);
+    // shading .1 + .9 |N.d|, N = g / |g + 1e-4| (deviceCode.cpp:285,294)
+    const float ex = s.gx + 1e-4f, ey = s.gy + 1e-4f, ez = s.gz + 1e-4f;
+    const float len = sqrtf(fmaf(ez, ez, fmaf(ey, ey, ex * ex)));
+    const float gd = fmaf(s.gz, r.d[2], fmaf(s.gy, r.d[1], s.gx * r.d[0]));
+    const float shade = fmaf(0.9f, fabsf(gd / len), 0.1f);
+    const float4 c = tf_lookup(tf_s, n_tf, nf, s.value);
+    // front-to-back compositing (deviceCode.cpp:292-296)
+    const float oma = 1.0f - color.w;
+    const float s1 = oma * c.w;
+    color.x = fmaf(s1 * c.x, shade, color.x);
+    color.y = fmaf(s1 * c.y, shade, color.y);
+    color.z = fmaf(s1 * c.z, shade, color.z);
+    color.w = fmaf(oma, c.w, color.w);
+  }
+  return n;
+}
+
+__device__ __forceinline__ float saturatef_(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+
+// temperature_to_rgb (deviceCode.cpp:300-314).
+__device__ __forceinline__ void heat_color(float t, float out[3]) {
+  const float K = 4.0f / 6.0f;
+  const float h = K - K * t;
+  const float v = 0.5f + 0.5f * t;
+  const float s = saturatef_(h) * 6.0f;
+  out[0] = v * saturatef_(fabsf(s - 3.0f) - 1.0f);
+  out[1] = v * saturatef_(2.0f - fabsf(s - 2.0f));
+  out[2] = v * saturatef_(2.0f - fabsf(s - 4.0f));
+}
+
+__device__ __forceinline__ uint32_t quantize8(float x) {
+  const float c = fminf(fmaxf(x, 0.0f), 1.0f);
+  return (uint32_t)(c * 255.0f + 0.5f);
+}
+
+__device__ __forceinline__ uint32_t pack_rgba(float4 c) {
+  return quantize8(c.x) | (quantize8(c.y) << 8) | (quantize8(c.z) << 16) | (quantize8(c.w) << 24);
+}
+
+// Loads the transfer function into shared memory with two zero entries on
+// each side (border addressing).
+__device__ __forceinline__ void load_tf(float4* tf_s, const float4* __restrict__ tf, int n) {
+  for (int i = threadIdx.x; i < n + 4; i += blockDim.x) {
+    const int k = i - 2;
+    tf_s[i] = (k >= 0 && k < n) ? __ldg(tf + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+// One pixel of one view: every virtual rank marches its bricks and runs
+// renderFrame's output stage; the rank images are blended front to back.
+// Returns the number of samples.
+__device__ __forceinline__ uint32_t render_pixel(const FrameArgs& a, const DevView& v, const float4* tf_s, int x,
+                                                 int y, uint32_t* fb_out, size_t fb_index) {
+  const int W = v.width, H = v.height;
+  const int pixel = x + W * y;
+  const size_t npx = (size_t)W * H;
+  const int R = v.n_ranks;
+  const int* __restrict__ order = a.sched + v.sched;
+  const int* __restrict__ rstart = order + R;
+  const int* __restrict__ rbricks = rstart + R + 1;
+  bool in_island = true;
+  if (a.num_islands > 1) {
+    const int tiles_x = (W + 15) / 16;
+    in_island = (((x >> 4) + tiles_x * (y >> 4)) % a.num_islands) == a.island_id;
+  }
+  const Ray ray = generate_ray(v, x, y);
+  float4 comp = make_float4(0.f, 0.f, 0.f, 0.f);
+  uint32_t comp8[4] = {0u, 0u, 0u, 0u};
+  uint32_t total = 0;
+  for (int k = 0; k < R; ++k) {
+    const int r = __ldg(order + k);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    float z = 1.0f;
+    uint32_t ns = 0;
+    if (in_island) {
+      uint32_t draw = 0;
+      const int j0 = __ldg(rstart + r), j1 = __ldg(rstart + r + 1);
+      for (int s = 0; s < a.spp; ++s) {
+        float4 color = make_float4(0.f, 0.f, 0.f, 0.f);
+        float tmin = 0.0f;
+        for (int j = j0; j < j1; ++j) {
+          const DevBrick b = a.bricks[__ldg(rbricks + j)];
+          float t0, t1;
+          if (!slab(ray, b.space_lo, b.space_hi, tmin, 1e10f, t0, t1)) continue;
+          const float ils = jitter(a.jitter_mode, a.jitter_value, (uint32_t)pixel, (uint32_t)a.accum_id, draw++);
+          const float tnear = (t0 > tmin ? t0 : 0.0f) + tmin;
+          z = fminf(z, tnear / v.max_depth);
+          ns += march_brick(b, tf_s, a.n_tf, ray, t0, t1, ils, a.dt, a.et_alpha, color);
+          tmin = t1 + 1e-20f;
+          if (!(color.w < a.et_alpha)) break;
+        }
+        acc.x = acc.x + color.x;
+        acc.y = acc.y + color.y;
+        acc.z = acc.z + color.z;
+        acc.w = acc.w + color.w;
+      }
+    }
+    if (a.heat_map) {
+      float hc[3];
+      heat_color((float)ns * (a.heat_map_scale / (float)a.spp), hc);
+      acc.x = fmaf(0.5f, acc.x, hc[0]);
+      acc.y = fmaf(0.5f, acc.y, hc[1]);
+      acc.z = fmaf(0.5f, acc.z, hc[2]);
+      acc.w = fmaf(0.5f, acc.w, 0.5f);
+    }
+    if (a.accum) {
+      float4* ap = a.accum + ((size_t)r * npx + pixel);
+      if (a.accum_id > 0) {
+        const float4 old = *ap;
+        acc.x = acc.x + old.x;
+        acc.y = acc.y + old.y;
+        acc.z = acc.z + old.z;
+        acc.w = acc.w + old.w;
+      }
+      if (a.accumulate) *ap = acc;
+    }
+    const float scale = 1.0f / (float)(a.accum_id + 1);
+    acc.x = acc.x * scale;
+    acc.y = acc.y * scale;
+    acc.z = acc.z * scale;
+    acc.w = acc.w * scale;
+    if (a.crosshair && (x == W / 2 || y == H / 2)) {
+      acc.x = 1.0f - acc.x;
+      acc.y = 1.0f - acc.y;
+      acc.z = 1.0f - acc.z;
+      acc.w = 1.0f - acc.w;
+    }
+    const float inv_spp = 1.0f / (float)a.spp;
+    const float4 img = make_float4(acc.x * inv_spp, acc.y * inv_spp, acc.z * inv_spp, acc.w * inv_spp);
+    if (a.rank_images) a.rank_images[(size_t)r * npx + pixel] = img;
+    if (a.rank_depth) a.rank_depth[(size_t)r * npx + pixel] = z;
+    if (a.composite_mode == ALOHA_COMPOSITE_UBYTE) {
+      const uint32_t q0 = quantize8(img.x), q1 = quantize8(img.y), q2 = quantize8(img.z), q3 = quantize8(img.w);
+      const uint32_t f = 255u - comp8[3];
+      comp8[0] = min(255u, comp8[0] + (q0 * f + 127u) / 255u);
+      comp8[1] = min(255u, comp8[1] + (q1 * f + 127u) / 255u);
+      comp8[2] = min(255u, comp8[2] + (q2 * f + 127u) / 255u);
+      comp8[3] = min(255u, comp8[3] + (q3 * f + 127u) / 255u);
+    } else {
+      const float oma = 1.0f - comp.w;
+      comp.x = fmaf(oma, img.x, comp.x);
+      comp.y = fmaf(oma, img.y, comp.y);
+      comp.z = fmaf(oma, img.z, comp.z);
+      comp.w = fmaf(oma, img.w, comp.w);
+    }
+    total += ns;
+  }
+  if (fb_out) {
+    fb_out[fb_index] = (a.composite_mode == ALOHA_COMPOSITE_UBYTE)
+                           ? (comp8[0] | (comp8[1] << 8) | (comp8[2] << 16) | (comp8[3] << 24))
+                           : pack_rgba(comp);
+  }
+  if (a.pixel_samples) a.pixel_samples[pixel] = total;
+  return total;
+}
+
+// Warp-aggregated add of per-thread sample counts into a 64-bit counter.
+__device__ __forceinline__ void count_samples(unsigned long long* counter, uint32_t n) {
+  if (!counter) return;
+  const unsigned s = __reduce_add_sync(0xffffffffu, n);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(counter, (unsigned long long)s);
+}
+
+}  // namespace aloha

@@ -1,0 +1,219 @@
+// order.cpp -- virtual-rank partition and per-view visibility order (host).
+//
+// partition_kd restates Partitioner::partitionKD (waikikiRenderer.cpp:150-270)
+// and kd_order its computeCompositeOrder (281-316).  face_order is this
+// library's default order: a separating-plane tree built from actual brick
+// faces, which stays correct for bricks whose faces are not at the KD
+// midplanes (the reference's midplane test can mis-order uneven bricks).
+#include "order.h"
+
+#include <algorithm>
+#include <climits>
+
+namespace aloha {
+
+bool partition_kd(const std::vector<Box>& boxes, int n_ranks, std::vector<int>& brick_rank,
+                  std::vector<KdNode>& tree) {
+  struct Group {
+    Box bounds;
+    std::vector<int> ids;
+    int node;
+  };
+  auto grow = [&](Box& b, int id) {
+    for (int a = 0; a < 3; ++a) {
+      b.lo[a] = std::min(b.lo[a], boxes[id].lo[a]);
+      b.hi[a] = std::max(b.hi[a], boxes[id].hi[a]);
+    }
+  };
+  const int n = (int)boxes.size();
+  const size_t quota = (size_t)(n / n_ranks);
+  Group root{Box::empty(), {}, 0};
+  for (int i = 0; i < n; ++i) {
+    grow(root.bounds, i);
+    root.ids.push_back(i);
+  }
+  tree.assign(1, KdNode{0, 0.f, INT_MAX, INT_MAX});
+  std::vector<Group> pending{root}, done;
+  // With n_ranks <= bricks and bricks that tile space every split makes
+  // progress; the cap turns a non-progressing split (which the reference
+  // would repeat forever) into an error.
+  size_t steps = 0;
+  while (!pending.empty()) {
+    if (++steps > 64 * boxes.size() + 64) return false;
+    // the group with the most bricks (first one on ties)
+    size_t pick = 0, most = 0;
+    for (size_t k = 0; k < pending.size(); ++k)
+      if (pending[k].ids.size() > most) {
+        most = pending[k].ids.size();
+        pick = k;
+      }
+    Group g = pending[pick];
+    pending.erase(pending.begin() + (long)pick);
+    if (g.ids.size() <= quota || done.size() == (size_t)n_ranks - 1) {
+      const int rank = (int)done.size();
+      tree[g.node].child1 = tree[g.node].child2 = ~rank;
+      done.push_back(g);
+      if (done.size() == (size_t)n_ranks) {
+        for (const Group& rest : pending) done.back().ids.insert(done.back().ids.end(), rest.ids.begin(), rest.ids.end());
+        pending.clear();
+        break;
+      }
+      continue;
+    }
+    float ext[3];
+    for (int a = 0; a < 3; ++a) ext[a] = g.bounds.hi[a] - g.bounds.lo[a];
+    int axis = 0;
+    if (ext[1] > ext[0] && ext[1] >= ext[2])
+      axis = 1;
+    else if (ext[2] > ext[0] && ext[2] >= ext[1])
+      axis = 2;
+    const float plane = g.bounds.lo[axis] + ext[axis] * 0.5f;
+    Group lo{Box::empty(), {}, 0}, hi{Box::empty(), {}, 0};
+    for (int id : g.ids) {
+      Group& side = ((boxes[id].lo[axis] + boxes[id].hi[axis]) / 2.f < plane) ? lo : hi;
+      grow(side.bounds, id);
+      side.ids.push_back(id);
+    }
+    tree[g.node].axis = axis;
+    tree[g.node].plane = plane;
+    lo.node = (int)tree.size();
+    tree[g.node].child1 = lo.node;
+    tree.push_back(KdNode{0, 0.f, INT_MAX, INT_MAX});
+    pending.push_back(lo);
+    hi.node = (int)tree.size();
+    tree[g.node].child2 = hi.node;
+    tree.push_back(KdNode{0, 0.f, INT_MAX, INT_MAX});
+    pending.push_back(hi);
+  }
+  brick_rank.assign(n, -1);
+  for (size_t r = 0; r < done.size(); ++r)
+    for (int id : done[r].ids) brick_rank[id] = (int)r;
+  return true;
+}
+
+std::vector<int> kd_order(const std::vector<KdNode>& tree, const float eye[3]) {
+  std::vector<int> order;
+  if (tree.empty()) return order;
+  std::vector<int> stack{0};
+  int at = 0;
+  while (!stack.empty()) {
+    const KdNode& nd = tree[at];
+    if (nd.child1 < 0 && nd.child2 < 0) {
+      order.push_back(~nd.child1);
+      at = stack.back();
+      stack.pop_back();
+    } else if (nd.child1 == INT_MAX) {
+      at = stack.back();
+      stack.pop_back();
+    } else {
+      const bool low_first = eye[nd.axis] < nd.plane;
+      at = low_first ? nd.child1 : nd.child2;
+      stack.push_back(low_first ? nd.child2 : nd.child1);
+    }
+  }
+  return order;
+}
+
+std::vector<int> face_order(const std::vector<Box>& item_bounds, const std::vector<char>& item_has_boxes,
+                            const float eye[3]) {
+  const int n = (int)item_bounds.size();
+  std::vector<int> order;
+  std::vector<std::vector<int>> work;
+  std::vector<int> all(n);
+  for (int i = 0; i < n; ++i) all[i] = i;
+  work.push_back(all);
+  while (!work.empty()) {
+    std::vector<int> items = std::move(work.back());
+    work.pop_back();
+    if (items.size() <= 1) {
+      order.insert(order.end(), items.begin(), items.end());
+      continue;
+    }
+    bool split = false;
+    for (int a = 0; a < 3 && !split; ++a) {
+      std::vector<float> planes;
+      for (int it : items)
+        if (item_has_boxes[it]) {
+          planes.push_back(item_bounds[it].lo[a]);
+          planes.push_back(item_bounds[it].hi[a]);
+        }
+      std::sort(planes.begin(), planes.end());
+      planes.erase(std::unique(planes.begin(), planes.end()), planes.end());
+      for (float p : planes) {
+        std::vector<int> below, above;
+        bool separates = true;
+        for (int it : items) {
+          if (!item_has_boxes[it] || item_bounds[it].hi[a] <= p)
+            below.push_back(it);
+          else if (item_bounds[it].lo[a] >= p)
+            above.push_back(it);
+          else {
+            separates = false;
+            break;
+          }
+        }
+        if (!separates || below.empty() || above.empty()) continue;
+        // the eye's side comes first (pushed last)
+        if (eye[a] < p) {
+          work.push_back(std::move(above));
+          work.push_back(std::move(below));
+        } else {
+          work.push_back(std::move(below));
+          work.push_back(std::move(above));
+        }
+        split = true;
+        break;
+      }
+    }
+    if (!split) {
+      std::vector<std::pair<float, int>> byd;
+      for (int it : items) {
+        float d2 = 0.f;
+        for (int a = 0; a < 3; ++a) {
+          const float c = item_has_boxes[it] ? (item_bounds[it].lo[a] + item_bounds[it].hi[a]) * 0.5f : eye[a];
+          d2 += (c - eye[a]) * (c - eye[a]);
+        }
+        byd.push_back({d2, it});
+      }
+      std::stable_sort(byd.begin(), byd.end(), [](const std::pair<float, int>& l, const std::pair<float, int>& r) {
+        return l.first < r.first;
+      });
+      for (auto& e : byd) order.push_back(e.second);
+    }
+  }
+  return order;
+}
+
+Schedule make_schedule(const std::vector<Box>& bricks, const std::vector<int>& brick_rank, int n_ranks,
+                       const std::vector<KdNode>& tree, int order_mode, const float eye[3]) {
+  const int nb = (int)bricks.size();
+  Schedule s;
+  // brick order: every brick is its own item
+  std::vector<char> has(nb, 1);
+  std::vector<int> border = face_order(bricks, has, eye);
+  // rank order
+  if (order_mode == ALOHA_ORDER_REFERENCE_KD && !tree.empty()) {
+    s.rank_order = kd_order(tree, eye);
+  } else {
+    std::vector<Box> rb(n_ranks, Box::empty());
+    std::vector<char> rhas(n_ranks, 0);
+    for (int b = 0; b < nb; ++b) {
+      const int r = brick_rank[b];
+      rhas[r] = 1;
+      for (int a = 0; a < 3; ++a) {
+        rb[r].lo[a] = std::min(rb[r].lo[a], bricks[b].lo[a]);
+        rb[r].hi[a] = std::max(rb[r].hi[a], bricks[b].hi[a]);
+      }
+    }
+    s.rank_order = face_order(rb, rhas, eye);
+  }
+  s.rank_start.assign(1, 0);
+  for (int r = 0; r < n_ranks; ++r) {
+    for (int b : border)
+      if (brick_rank[b] == r) s.rank_bricks.push_back(b);
+    s.rank_start.push_back((int)s.rank_bricks.size());
+  }
+  return s;
+}
+
+}  // namespace aloha

@@ -1,0 +1,204 @@
+// render.cu -- forward kernels: fused per-view render, persistent batched
+// render, ordered-over composite, brick padding.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "internal.h"
+#include "march.cuh"
+
+namespace aloha {
+
+// Ray tiles: a CTA covers TW x TH pixels; each warp an 8 x 4 block, so the 32
+// rays of a warp start within a few voxels of each other and walk the same
+// cache lines.
+template <int TW, int TH>
+struct TileMap {
+  static constexpr int kThreads = TW * TH;
+  static constexpr int kWarpsX = TW / 8;
+  __device__ __forceinline__ static void pixel(int tid, int& px, int& py) {
+    const int w = tid >> 5, lane = tid & 31;
+    px = (w % kWarpsX) * 8 + (lane & 7);
+    py = (w / kWarpsX) * 4 + (lane >> 3);
+  }
+};
+
+template <int TW, int TH>
+__global__ void __launch_bounds__(TW* TH) render_view_kernel(FrameArgs a, int view) {
+  extern __shared__ float4 tf_s[];
+  load_tf(tf_s, a.tf, a.n_tf);
+  __syncthreads();
+  const DevView v = a.views[view];
+  int px, py;
+  TileMap<TW, TH>::pixel(threadIdx.x, px, py);
+  const int x = blockIdx.x * TW + px, y = blockIdx.y * TH + py;
+  uint32_t n = 0;
+  if (x < v.width && y < v.height) n = render_pixel(a, v, tf_s, x, y, a.fb, (size_t)x + (size_t)v.width * y);
+  count_samples(a.counter, n);
+}
+
+// Persistent batched render: CTAs pull ray tiles of all batch items from one
+// atomic counter until the batch is done (no waiting on other CTAs).
+template <int TW, int TH>
+__global__ void __launch_bounds__(TW* TH) render_batch_kernel(BatchArgs b) {
+  extern __shared__ float4 tf_s[];
+  __shared__ int s_tile;
+  load_tf(tf_s, b.f.tf, b.f.n_tf);
+  int px, py;
+  TileMap<TW, TH>::pixel(threadIdx.x, px, py);
+  uint32_t n = 0;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(b.work_counter, 1u);
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= b.total_tiles) break;
+    // item = last index with tile_prefix[item] <= tile
+    int lo = 0, hi = b.n_items - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(b.tile_prefix + mid) <= tile)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const int item = lo;
+    const DevView v = b.f.views[__ldg(b.view_ids + item)];
+    const int tiles_x = (v.width + TW - 1) / TW;
+    const int local = tile - __ldg(b.tile_prefix + item);
+    const int x = (local % tiles_x) * TW + px, y = (local / tiles_x) * TH + py;
+    if (x < v.width && y < v.height)
+      n += render_pixel(b.f, v, tf_s, x, y, b.fbs[item], (size_t)x + (size_t)v.width * y);
+  }
+  count_samples(b.f.counter, n);
+}
+
+// Ordered "over" of per-rank float images (IceT BLEND with ORDERED_COMPOSITE,
+// waikikiRenderer.cpp:910-917,1042-1079), front to back.
+__global__ void composite_f32_kernel(const float4* __restrict__ imgs, const int* __restrict__ order, int n_ranks,
+                                     int npx, int mode, uint32_t* __restrict__ fb) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npx; p += gridDim.x * blockDim.x) {
+    float4 comp = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t c8[4] = {0u, 0u, 0u, 0u};
+    for (int k = 0; k < n_ranks; ++k) {
+      const int r = __ldg(order + k);
+      const float4 img = __ldg(imgs + (size_t)r * npx + p);
+      if (mode == ALOHA_COMPOSITE_UBYTE) {
+        const uint32_t q0 = quantize8(img.x), q1 = quantize8(img.y), q2 = quantize8(img.z), q3 = quantize8(img.w);
+        const uint32_t f = 255u - c8[3];
+        c8[0] = min(255u, c8[0] + (q0 * f + 127u) / 255u);
+        c8[1] = min(255u, c8[1] + (q1 * f + 127u) / 255u);
+        c8[2] = min(255u, c8[2] + (q2 * f + 127u) / 255u);
+        c8[3] = min(255u, c8[3] + (q3 * f + 127u) / 255u);
+      } else {
+        const float oma = 1.0f - comp.w;
+        comp.x = fmaf(oma, img.x, comp.x);
+        comp.y = fmaf(oma, img.y, comp.y);
+        comp.z = fmaf(oma, img.z, comp.z);
+        comp.w = fmaf(oma, img.w, comp.w);
+      }
+    }
+    fb[p] = (mode == ALOHA_COMPOSITE_UBYTE) ? (c8[0] | (c8[1] << 8) | (c8[2] << 16) | (c8[3] << 24))
+                                            : pack_rgba(comp);
+  }
+}
+
+// 8-bit ordered over of external RGBA8 rank images.
+__global__ void composite_u8_kernel(const uint32_t* __restrict__ imgs, const int* __restrict__ order, int n_ranks,
+                                    int npx, uint32_t* __restrict__ fb) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npx; p += gridDim.x * blockDim.x) {
+    uint32_t c8[4] = {0u, 0u, 0u, 0u};
+    for (int k = 0; k < n_ranks; ++k) {
+      const uint32_t q = __ldg(imgs + (size_t)__ldg(order + k) * npx + p);
+      const uint32_t f = 255u - c8[3];
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) c8[ch] = min(255u, c8[ch] + (((q >> (8 * ch)) & 255u) * f + 127u) / 255u);
+    }
+    fb[p] = c8[0] | (c8[1] << 8) | (c8[2] << 16) | (c8[3] << 24);
+  }
+}
+
+// Copies a brick (x fastest) into its padded array, filling the apron with
+// clamped edge values, and flags non-finite voxels.
+__global__ void pad_brick_kernel(const float* __restrict__ src, int nx, int ny, int nz, float* __restrict__ dst,
+                                 int px, int py, int pz, int* nonfinite) {
+  const size_t total = (size_t)px * py * pz;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % px);
+    const int y = (int)((i / px) % py);
+    const int z = (int)(i / ((size_t)px * py));
+    const int sx = min(max(x - kApron, 0), nx - 1);
+    const int sy = min(max(y - kApron, 0), ny - 1);
+    const int sz = min(max(z - kApron, 0), nz - 1);
+    const float v = src[((size_t)sz * ny + sy) * nx + sx];
+    if (!isfinite(v)) atomicOr(nonfinite, 1);
+    dst[i] = v;
+  }
+}
+
+static size_t tf_smem(int n_tf) { return (size_t)(n_tf + 4) * sizeof(float4); }
+
+cudaError_t launch_render(const FrameArgs& a, int view, int width, int height, cudaStream_t s) {
+  constexpr int TW = 16, TH = 8;
+  dim3 grid((width + TW - 1) / TW, (height + TH - 1) / TH);
+  render_view_kernel<TW, TH><<<grid, TW * TH, tf_smem(a.n_tf), s>>>(a, view);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_render_batch(const BatchArgs& b, int tile_w, int tile_h, int grid, cudaStream_t s) {
+  const size_t smem = tf_smem(b.f.n_tf);
+  if (tile_w == 8 && tile_h == 8)
+    render_batch_kernel<8, 8><<<grid, 64, smem, s>>>(b);
+  else if (tile_w == 16 && tile_h == 8)
+    render_batch_kernel<16, 8><<<grid, 128, smem, s>>>(b);
+  else if (tile_w == 32 && tile_h == 4)
+    render_batch_kernel<32, 4><<<grid, 128, smem, s>>>(b);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+int batch_blocks_per_sm(int tile_w, int tile_h, int n_tf) {
+  int n = 0;
+  const size_t smem = tf_smem(n_tf);
+  cudaError_t e = cudaErrorInvalidValue;
+  if (tile_w == 8 && tile_h == 8)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_batch_kernel<8, 8>, 64, smem);
+  else if (tile_w == 16 && tile_h == 8)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_batch_kernel<16, 8>, 128, smem);
+  else if (tile_w == 32 && tile_h == 4)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_batch_kernel<32, 4>, 128, smem);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+static int composite_grid(int npx) {
+  int g = (npx + 255) / 256;
+  return g < 1 ? 1 : (g > 152 * 16 ? 152 * 16 : g);
+}
+
+cudaError_t launch_composite_f32(const float4* imgs, const int* order, int n_ranks, int npx, int mode, uint32_t* fb,
+                                 cudaStream_t s) {
+  composite_f32_kernel<<<composite_grid(npx), 256, 0, s>>>(imgs, order, n_ranks, npx, mode, fb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_composite_u8(const uint32_t* imgs, const int* order, int n_ranks, int npx, uint32_t* fb,
+                                cudaStream_t s) {
+  composite_u8_kernel<<<composite_grid(npx), 256, 0, s>>>(imgs, order, n_ranks, npx, fb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pad_brick(const float* src, int nx, int ny, int nz, float* dst, int px, int py, int pz,
+                             int* nonfinite, cudaStream_t s) {
+  const size_t total = (size_t)px * py * pz;
+  size_t g = (total + 255) / 256;
+  if (g > 152 * 64) g = 152 * 64;
+  if (g < 1) g = 1;
+  pad_brick_kernel<<<(unsigned)g, 256, 0, s>>>(src, nx, ny, nz, dst, px, py, pz, nonfinite);
+  return cudaGetLastError();
+}
+
+}  // namespace aloha

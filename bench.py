@@ -1,0 +1,424 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 volume hot path on the sort-last workload.
+
+Workload (one frame = one step): a 512^3 fp32 field of 64 seeded Gaussian
+blobs, split by chopSuey into 2x2x2 bricks (8 bricks with a one-voxel upper
+ghost layer, 540 MB resident in HBM), rendered as 8 virtual ranks at
+1024x1024 with 256 seeded orbit cameras; every rank marches its brick and the
+rank images are blended front to back in fp32.  Step 0.5 voxel, early
+termination at alpha 0.99, 256-entry ramp transfer function.
+
+Prints one JSON line (rank 0).  `value` = Gsamples/s (march loop-body
+executions per second) with everything resident in HBM; `e2e` = the same
+metric through the public C ABI with a pinned host frame buffer (camera in,
+frame out every step).  `--impl reference` times the CPU restatement of the
+reference path (the reference's own build cannot be compiled here) on the
+host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gsamples/s & ms/frame (fwd; fwd+adjoint) 512³ DVR @1024² on 1 GB300 vs plain"
+WORKLOAD = ("sort-last DVR: 512^3 fp32 64-blob field, chopSuey 2x2x2 (8 bricks, 8 virtual ranks), "
+            "1024x1024, 256 orbit cameras, dt 0.5, ET 0.99, fp32 ordered-over composite")
+DEVVIEW_BYTES = 80
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=256)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["aloha", "reference"], default="aloha")
+    ap.add_argument("--n", type=int, default=512, help="volume edge (voxels)")
+    ap.add_argument("--size", type=int, default=1024, help="image edge (pixels)")
+    ap.add_argument("--cameras", type=int, default=256)
+    ap.add_argument("--batch-views", type=int, default=64)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU work of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="short run for ncu (no baselines, no clocks)")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ helpers
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str):
+    """dram bytes per launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}.traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+def build_scene(args, device):
+    from aloha_gb300 import scenes as S
+    from aloha_gb300 import volfile as V
+    n = args.n
+    vol = S.blob_field((n, n, n), 64, (n / 16.0, n / 6.4), seed=2001, device=device)
+    descs = V.chopsuey_split((n, n, n), 8)
+    vox = [V.brick_voxels(vol, d) for d in descs]
+    tf = S.ramp_tf()
+    cams = S.orbit_cameras((n, n, n), args.cameras, args.size, args.size, seed=2002)
+    return vol, descs, vox, tf, cams
+
+
+def bricks_hit(descs, cam, W, H, stride=8):
+    """Bricks whose space box any (subsampled) pixel ray enters."""
+    org, d00, du, dv = (np.asarray(c, np.float64) for c in cam)
+    ys, xs = np.meshgrid(np.arange(0, H, stride) + 0.5, np.arange(0, W, stride) + 0.5, indexing="ij")
+    dirs = d00[None, None] + xs[..., None] * du + ys[..., None] * dv
+    dirs /= np.linalg.norm(dirs, axis=-1, keepdims=True)
+    dirs = np.where(np.abs(dirs) < 1e-5, 1e-5, dirs)
+    hit = []
+    for k, d in enumerate(descs):
+        lo = (np.asarray(d["space_lo"]) - org) / dirs
+        hi = (np.asarray(d["space_hi"]) - org) / dirs
+        t0 = np.maximum(np.minimum(lo, hi).max(-1), 0)
+        t1 = np.maximum(lo, hi).min(-1)
+        if np.any(t0 < t1):
+            hit.append(k)
+    return hit
+
+
+def algorithmic_bytes(descs, hit, n_tf, W, H):
+    vox = sum(np.prod([descs[k]["voxel_hi"][a] - descs[k]["voxel_lo"][a] for a in range(3)]) for k in hit)
+    return int(vox) * 4 + n_tf * 16 + W * H * 4
+
+
+# --------------------------------------------------------------- CPU arms
+
+def cpu_render_sample(descs, vox_np, tf, cams, W, H, target_s, threads=0, max_views=None):
+    """Oracle (CPU restatement, OpenMP over rows) on a bounded sample of rows
+    of the first views; returns (samples, seconds, rows, views, threads)."""
+    from oracle import oracle as O
+    O.lib()
+    n_thr = threads or O.lib().ora_max_threads()
+    params = O.make_params()
+    scheds = {}
+    total_s, total_samples, rows_done, views_used = 0.0, 0, 0, set()
+    # bands of 16 rows spread over the image (one OpenMP row per thread), views
+    # in order, until the time target
+    band = 16
+    per_view_rows = list(range(0, H, H // 8))
+    for vi, cam in enumerate(cams if max_views is None else cams[:max_views]):
+        c = O.make_camera(*cam)
+        if vi not in scheds:
+            scheds[vi] = O.schedule(descs, 8, list(c.org))
+        for y in per_view_rows:
+            t0 = time.perf_counter()
+            r = O.render(descs, vox_np, tf, c, W, H, params, sched=scheds[vi], rows=(y, min(H, y + band)),
+                         threads=n_thr, want=())
+            total_s += time.perf_counter() - t0
+            total_samples += r["samples"]
+            rows_done += min(H, y + band) - y
+            views_used.add(vi)
+            if total_s >= target_s:
+                return total_samples, total_s, rows_done, len(views_used), n_thr
+    return total_samples, total_s, rows_done, len(views_used), n_thr
+
+
+def reference_arm(args):
+    """--impl reference: the CPU restatement of the reference path on all host
+    cores (the reference's OptiX/MPI/IceT build is unavailable), rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from aloha_gb300 import scenes as S
+    from aloha_gb300 import volfile as V
+    from oracle import oracle as O
+    n, W = args.n, args.size
+    vol = S.blob_field((n, n, n), 64, (n / 16.0, n / 6.4), seed=2001)
+    descs = V.chopsuey_split((n, n, n), 8)
+    vox = [V.brick_voxels(vol, d) for d in descs]
+    tf = S.ramp_tf()
+    cams = S.orbit_cameras((n, n, n), args.cameras, W, W, seed=2002)
+    threads = O.lib().ora_max_threads()
+    params = O.make_params()
+    rows_per_step = 16
+
+    def step(k):
+        cam = O.make_camera(*cams[k % len(cams)])
+        sch = O.schedule(descs, 8, list(cam.org))
+        y0 = (k * 131) % (W - rows_per_step)
+        r = O.render(descs, vox, tf, cam, W, W, params, sched=sch, rows=(y0, y0 + rows_per_step),
+                     threads=threads, want=())
+        return r["samples"]
+
+    for k in range(args.warmup):
+        step(k)
+    t0 = time.perf_counter()
+    samples = 0
+    for k in range(args.steps):
+        samples += step(args.warmup + k)
+    dt = time.perf_counter() - t0
+    g = samples / dt / 1e9
+    line = {"metric": METRIC, "value": g, "unit": "Gsamples/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "step": f"{rows_per_step} rows of one 1024-wide view"},
+            "cpu_baseline": {"value": g, "unit": "Gsamples/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} steps x {rows_per_step} rows x {W} pixels"},
+            "e2e": {"value": g, "unit": "Gsamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    import torch
+    import torch.distributed as dist
+
+    from aloha_gb300 import abi
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    vol, descs, vox, tf, cams = build_scene(args, dev)
+    W = H = args.size
+    ctx = abi.Context(local)
+    ctx.set_bricks(descs, vox)
+    ctx.set_transfer_function(tf)
+    ctx.set_ranks(8)
+    ctx.set_params()
+    # replicas only: rank r renders cameras r, r+N, ...
+    mine = list(range(rank, len(cams), world))
+    stream = torch.cuda.Stream(device=dev)
+    fb = torch.zeros((H, W), dtype=torch.int32, device=dev)
+
+    # per-camera sample counts and algorithmic bytes (untimed)
+    samples_of, bytes_of = {}, {}
+    with torch.cuda.stream(stream):
+        for ci in mine:
+            ctx.set_camera(0, *cams[ci])
+            ctx.resize(0, W, H)
+            ctx.render(0, fb, stream)
+            samples_of[ci] = ctx.stats().samples
+            bytes_of[ci] = algorithmic_bytes(descs, bricks_hit(descs, cams[ci], W, H), tf.shape[0], W, H)
+
+    steps = [mine[k % len(mine)] for k in range(args.steps)]
+    for k in range(args.warmup):
+        ctx.set_camera(0, *cams[mine[k % len(mine)]])
+        ctx.render(0, fb, stream)
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in steps]
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        t_start.record(stream)
+        for (e0, e1), ci in zip(ev, steps):
+            ctx.set_camera(0, *cams[ci])
+            e0.record(stream)
+            ctx.render(0, fb, stream)
+            e1.record(stream)
+        t_end.record(stream)
+        barrier()
+    elapsed_ms = t_start.elapsed_time(t_end)
+    launch_ms = [e0.elapsed_time(e1) for e0, e1 in ev]
+    total_samples = sum(samples_of[ci] for ci in steps)
+    if world > 1:
+        t = torch.tensor([elapsed_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+        s = torch.tensor([total_samples], dtype=torch.float64, device=dev)
+        dist.all_reduce(s)
+        total_samples = int(s.item())
+    value = total_samples / (elapsed_ms * 1e-3) / 1e9
+
+    # roofline of the fused render kernel: algorithmic bytes / launch duration
+    mean_bytes = float(np.mean([bytes_of[ci] for ci in steps]))
+    mean_launch = float(np.mean(launch_ms))
+    peak, peak_kind = measured_peaks()
+    achieved = mean_bytes / (mean_launch * 1e-3) / 1e9
+    traffic = profile_traffic("render_view_kernel")
+
+    result = {"metric": METRIC, "value": value, "unit": "Gsamples/s", "n_gpus": world, "steps": args.steps,
+              "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+              "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+              "config": {"workload": WORKLOAD, "volume": [args.n] * 3, "bricks": 8, "virtual_ranks": 8,
+                         "image": [W, H], "cameras": len(cams), "parallelism": f"replicas x{world} (views)",
+                         "l2": "inputs larger than L2 (540 MB of bricks per view)"},
+              "ms_per_frame": elapsed_ms / args.steps,
+              "samples_per_frame": total_samples / max(1, args.steps * world),
+              "gpu_launches": args.steps,
+              "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                           "frac": achieved / peak, "peak_kind": peak_kind,
+                           "traffic": traffic["bytes_per_launch"] if traffic else None,
+                           "kernel": "render_view_kernel<16,8>",
+                           "algorithmic_bytes_per_launch": mean_bytes, "launch_ms": mean_launch}}
+    clocks = clk.summary()
+    if clocks:
+        result["clocks"] = clocks
+
+    if not args.profile:
+        # e2e: through the C ABI with a pinned host frame buffer every step
+        fb_host = torch.zeros((H, W), dtype=torch.int32).pin_memory()
+        for k in range(args.warmup):
+            ctx.set_camera(0, *cams[mine[k % len(mine)]])
+            ctx.render(0, fb_host, stream)
+        barrier()
+        t0 = time.perf_counter()
+        for ci in steps:
+            ctx.set_camera(0, *cams[ci])
+            ctx.render(0, fb_host, stream)
+        barrier()
+        e2e_s = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([e2e_s], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        sched_bytes = 4 * (2 * 8 + 1 + 8)
+        result["e2e"] = {"value": total_samples / e2e_s / 1e9, "unit": "Gsamples/s",
+                         "ms_per_frame": e2e_s / args.steps * 1e3,
+                         "h2d_bytes_per_step": DEVVIEW_BYTES + sched_bytes, "d2h_bytes_per_step": W * H * 4}
+
+        if not args.no_batched and rank == 0:
+            result["batched"] = batched_section(ctx, cams, mine, W, H, args, stream, dev, samples_of)
+
+        if not args.no_cpu_baseline and rank == 0:
+            vol_np = vol.cpu().numpy()
+            from aloha_gb300 import volfile as V
+            vox_np = [V.brick_voxels(vol_np, d) for d in descs]
+            s, sec, rows, nv, thr = cpu_render_sample(descs, vox_np, tf, cams, W, H, args.cpu_seconds)
+            result["cpu_baseline"] = {"value": s / sec / 1e9, "unit": "Gsamples/s", "cores": thr, "kind": "port",
+                                      "sample": f"{rows} rows (16-row bands, 8 per view) of {nv} view(s) at {W} px, "
+                                                f"{s} samples in {sec:.1f} s"}
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def batched_section(ctx, cams, mine, W, H, args, stream, dev, samples_of):
+    """64 views in one persistent launch (CUDA graph) vs 64 plain launches."""
+    import torch
+    nv = min(args.batch_views, len(mine))
+    views = list(range(1, nv + 1))
+    for v, ci in zip(views, mine[:nv]):
+        ctx.set_camera(v, *cams[ci])
+        ctx.resize(v, W, H)
+    fbs = [torch.zeros((H, W), dtype=torch.int32, device=dev) for _ in views]
+    b = ctx.batch(views, fbs)
+    tw, th, _ = b.autotune(stream, reps=1)
+
+    def timed(fn, reps=3):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms_graph = timed(lambda: b.launch_graph(stream))
+
+    def plain():
+        for v, f in zip(views, fbs):
+            ctx.render(v, f, stream)
+
+    ms_plain = timed(plain)
+    samples = sum(samples_of[ci] for ci in mine[:nv])
+    b.close()
+    return {"views": nv, "tile": [tw, th], "ms_batch": ms_graph, "ms_plain_launches": ms_plain,
+            "speedup_vs_plain": ms_plain / ms_graph, "gsamples_per_s": samples / (ms_graph * 1e-3) / 1e9}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,191 @@
+/*
+ * aloha.h -- C ABI of the GB300 volume hot path (one GPU, bricks as virtual ranks).
+ *
+ * Replaces, for the volume path only:
+ *   - the renderer host API mpi::DistributedRenderer / maui::Renderer
+ *     (DistributedRenderer.h:29-71, waikikiRenderer.h:28-118): camera, resize,
+ *     colour map and render(fb) events;
+ *   - the OWL launch of the raygen renderFrame (waikikiRenderer.cpp:1021-1028,
+ *     deviceCode.cpp:340-421) with the brick march integrateBrick
+ *     (deviceCode.cpp:256-298);
+ *   - the IceT ordered BLEND composite of the per-rank images
+ *     (waikikiRenderer.cpp:895-917,1030-1079).
+ *
+ * Conventions: every call returns an aloha_status (0 = ALOHA_OK); the library
+ * never exits or traps.  Pointers may be host or device memory unless stated;
+ * when an output is host memory the call copies into it and returns after the
+ * stream has finished.  `stream` is a cudaStream_t (NULL = default stream).
+ * Calls on one context are not thread-safe and must not overlap on the GPU
+ * (the reference's renderer is single-threaded per rank as well).
+ */
+#ifndef ALOHA_GB300_ALOHA_H
+#define ALOHA_GB300_ALOHA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ALOHA_ABI_VERSION 1
+
+typedef enum {
+  ALOHA_OK = 0,
+  ALOHA_ERR_INVALID_ARGUMENT = 1, /* bad size, NaN camera, bad enum value */
+  ALOHA_ERR_NULL_POINTER = 2,
+  ALOHA_ERR_OUT_OF_RANGE = 3,     /* view / brick / rank index out of range */
+  ALOHA_ERR_NOT_READY = 4,        /* no bricks, transfer function or camera yet */
+  ALOHA_ERR_OUT_OF_MEMORY = 5,    /* request larger than free device memory */
+  ALOHA_ERR_CUDA = 6,             /* a CUDA runtime call failed (see aloha_last_error) */
+  ALOHA_ERR_TIMEOUT = 7,          /* a bounded device-side wait gave up */
+  ALOHA_ERR_MISSING_BRICK = 8,    /* a virtual rank has no data (brick never uploaded) */
+  ALOHA_ERR_UNSUPPORTED = 9
+} aloha_status;
+
+enum { ALOHA_JITTER_NONE = 0, ALOHA_JITTER_CONST = 1, ALOHA_JITTER_HASH = 2 };
+enum { ALOHA_COMPOSITE_FP32 = 0, ALOHA_COMPOSITE_UBYTE = 1 };
+enum { ALOHA_ORDER_FACES = 0, ALOHA_ORDER_REFERENCE_KD = 1 };
+
+typedef struct aloha_ctx aloha_ctx;
+
+/* One brick, byte-identical to a .vol brick header (chopSuey.cpp:342-345,
+ * read at waikikiRenderer.cpp:615-618; VolBrick fields deviceCode.h:35-50):
+ * cellRange, voxelRange (half-open, with chopSuey's upper ghost layer),
+ * spaceRange (voxel units), valueRange. */
+typedef struct {
+  int32_t cell_lo[3], cell_hi[3];
+  int32_t voxel_lo[3], voxel_hi[3];
+  float space_lo[3], space_hi[3];
+  float value_range[2];
+} aloha_brick_desc;
+
+/* Render settings (LaunchParams::render, deviceCode.h:90-95, plus the values
+ * the reference hard-codes: dt = 2 at waikikiRenderer.cpp:1023, ET .99 at
+ * deviceCode.cpp:270,391, crosshair always on at deviceCode.cpp:410-414). */
+typedef struct {
+  float dt;               /* step along the ray in voxels */
+  float et_alpha;         /* early ray termination threshold */
+  int32_t jitter_mode;    /* ALOHA_JITTER_*: ils_t0 = 0, jitter_value, or a hash of (pixel, accum_id, draw) */
+  float jitter_value;
+  int32_t crosshair;      /* invert column W/2 and row H/2 of each rank image */
+  int32_t spp;            /* samples per pixel (repeat the march, new jitter draws) */
+  int32_t accum_id;       /* progressive frame index; > 0 adds the accumulation buffer */
+  int32_t accumulate;     /* keep a per-view, per-rank float4 accumulation buffer */
+  int32_t heat_map;       /* blend a heat map of per-pixel sample counts */
+  float heat_map_scale;
+  int32_t composite_mode; /* ALOHA_COMPOSITE_FP32 (one rounding) or _UBYTE (RGBA8 blend, IceT-style) */
+  int32_t island_id;      /* image-parallel islands: 16x16 tiles with tile % num_islands == island_id */
+  int32_t num_islands;
+  int32_t order_mode;     /* ALOHA_ORDER_FACES or _REFERENCE_KD (midplane KD of partitionKD) */
+} aloha_render_params;
+
+typedef struct {
+  uint64_t samples;       /* march loop-body executions of the last render/batch call */
+  int32_t n_bricks;
+  int32_t n_ranks;
+  uint64_t brick_bytes;   /* device bytes held for bricks (padded layout) */
+} aloha_stats;
+
+int aloha_abi_version(void);
+const char* aloha_status_string(int status);
+
+/* Context = one renderer on one GPU (replaces maui::Renderer's constructor,
+ * waikikiRenderer.cpp:344-846, minus MPI/IceT/OWL set-up). */
+int aloha_create(int device, aloha_ctx** out);
+int aloha_destroy(aloha_ctx* ctx);
+const char* aloha_last_error(const aloha_ctx* ctx);
+
+int aloha_default_render_params(aloha_render_params* out);
+int aloha_set_render_params(aloha_ctx* ctx, const aloha_render_params* params);
+
+/* Upload `n` bricks (replaces the brick upload of waikikiRenderer.cpp:637-777).
+ * voxels[i] holds brick i's voxel range, x fastest, float32 (host or device).
+ * The library keeps its own device copy.  Resets the rank partition to one
+ * rank per brick. */
+int aloha_set_bricks(aloha_ctx* ctx, const aloha_brick_desc* descs, const float* const* voxels, int n);
+
+/* Replace one brick's voxels (same voxel range), e.g. after a density update. */
+int aloha_update_brick(aloha_ctx* ctx, int brick, const float* voxels);
+
+/* Mark one brick's data as lost (a virtual rank that went away): renders
+ * return ALOHA_ERR_MISSING_BRICK instead of an image without that brick,
+ * until aloha_update_brick supplies the data again.  No reference
+ * counterpart: the reference has no failure handling (Headless.cpp:52-57). */
+int aloha_drop_brick(aloha_ctx* ctx, int brick);
+
+/* Transfer function: n RGBA float entries (handleColorMapEvent,
+ * waikikiRenderer.cpp:945-1013). */
+int aloha_set_transfer_function(aloha_ctx* ctx, const float* rgba, int n);
+
+/* Virtual ranks: partitionKD of the bricks over n_ranks ranks
+ * (waikikiRenderer.cpp:150-270, called at 630-631), or an explicit
+ * assignment brick -> rank. */
+int aloha_set_ranks(aloha_ctx* ctx, int n_ranks);
+int aloha_set_rank_assignment(aloha_ctx* ctx, const int* brick_rank, int n_bricks, int n_ranks);
+
+/* Per-view camera and size (handleCameraEvent / handleResizeEvent,
+ * waikikiRenderer.cpp:853-920).  Views are numbered 0..4095. */
+int aloha_set_camera(aloha_ctx* ctx, int view, const float* org, const float* dir_00, const float* dir_du,
+                     const float* dir_dv);
+int aloha_resize(aloha_ctx* ctx, int view, int width, int height);
+
+/* Front-to-back rank order for a view (computeCompositeOrder,
+ * waikikiRenderer.cpp:281-316, or the face-based order). */
+int aloha_get_composite_order(aloha_ctx* ctx, int view, int* rank_order, int max_ranks, int* n_ranks);
+
+/* Render one view into an RGBA8 frame buffer of width*height uint32
+ * (Renderer::render, waikikiRenderer.cpp:1015-1080): all virtual ranks march
+ * their bricks and their images are composited in one fused kernel. */
+int aloha_render(aloha_ctx* ctx, int view, uint32_t* fb, void* stream);
+
+/* The unfused form: per-rank images after renderFrame's output stage
+ * (float RGBA, [n_ranks][height][width][4], indexed by rank id) and per-rank
+ * depth ([n_ranks][height][width], fbDepth of deviceCode.cpp:388,397;
+ * may be NULL). */
+int aloha_render_partials(aloha_ctx* ctx, int view, float* rank_images, float* rank_depth, void* stream);
+
+/* IceT stand-in: blend n_ranks float RGBA images front to back in `order`
+ * (ordered BLEND, waikikiRenderer.cpp:910-917,1042-1079) into RGBA8.  Mode
+ * ALOHA_COMPOSITE_FP32 blends in fp32 and rounds once; _UBYTE quantises each
+ * image first and blends in 8 bits.  Context-free. */
+int aloha_composite_over(const float* rank_images, const int* order, int n_ranks, int width, int height,
+                         int mode, uint32_t* fb, void* stream);
+
+/* IceT stand-in for external RGBA8 rank images ([n_ranks][height][width]
+ * uint32, premultiplied), blended in 8 bits front to back in `order`. */
+int aloha_composite_over_rgba8(const uint32_t* rank_fbs, const int* order, int n_ranks, int width, int height,
+                               uint32_t* fb, void* stream);
+
+int aloha_get_stats(aloha_ctx* ctx, aloha_stats* out);
+
+/* ---- Batched form: many views in one persistent launch (no reference
+ * counterpart; the reference renders one camera per launch,
+ * waikikiRenderer.cpp:1028).  A batch fixes a list of (view, device frame
+ * buffer) items; aloha_batch_launch only enqueues kernels and memsets, so it
+ * can be captured into a CUDA graph; aloha_batch_launch_graph captures it
+ * once and replays the graph.  Camera changes of the batch's views are picked
+ * up at the next launch. */
+typedef struct aloha_batch aloha_batch;
+
+int aloha_batch_create(aloha_ctx* ctx, const int* views, int n_items, uint32_t* const* fbs, aloha_batch** out);
+/* Ray-tile shape of the persistent kernel: 8x8, 16x8 or 32x4 pixels per CTA;
+ * ctas_per_sm = 0 picks the occupancy limit. */
+int aloha_batch_set_config(aloha_batch* b, int tile_w, int tile_h, int ctas_per_sm);
+int aloha_batch_get_config(const aloha_batch* b, int* tile_w, int* tile_h, int* ctas_per_sm);
+int aloha_batch_launch(aloha_batch* b, void* stream);
+int aloha_batch_launch_graph(aloha_batch* b, void* stream);
+/* Time every tile shape (`reps` launches each, CUDA events) and keep the
+ * fastest; returns its shape and mean milliseconds per launch. */
+int aloha_batch_autotune(aloha_batch* b, void* stream, int reps, int* tile_w, int* tile_h, float* ms);
+int aloha_batch_destroy(aloha_batch* b);
+
+/* Convenience: render n views (fbs may be host or device) in one batched
+ * launch and wait for it. */
+int aloha_render_batch(aloha_ctx* ctx, const int* views, int n_items, uint32_t* const* fbs, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ALOHA_GB300_ALOHA_H */

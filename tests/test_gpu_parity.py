@@ -1,0 +1,307 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+The CUDA kernels and the oracle share one fp32 evaluation order (explicit
+fused multiply-adds, no contraction), so frames, per-rank float images,
+depths and sample counts must be bit-identical.
+"""
+import numpy as np
+import pytest
+
+from aloha_gb300 import abi
+from aloha_gb300 import scenes as S
+from tests import scenes_for_tests as T
+
+pytestmark = pytest.mark.gpu
+
+
+def setup_ctx(make, descs, vox, tf, n_ranks=None, **params):
+    ctx = make()
+    ctx.set_bricks(descs, vox)
+    ctx.set_transfer_function(tf)
+    if n_ranks is not None:
+        ctx.set_ranks(n_ranks)
+    ctx.set_params(**params)
+    return ctx
+
+
+def oracle_frame(O, descs, vox, tf, cam, W, H, n_ranks=1, order_mode=0, want=("fb",), **params):
+    return O.render(descs, vox, tf, O.make_camera(*cam), W, H, O.make_params(**params), n_ranks=n_ranks,
+                    order_mode=order_mode, want=want)
+
+
+def gpu_frame(ctx, cam, W, H, view=0):
+    ctx.set_camera(view, *cam)
+    ctx.resize(view, W, H)
+    fb = ctx.render(view, width=W, height=H)
+    return fb, ctx.stats().samples
+
+
+def assert_same_fb(a, b):
+    if not np.array_equal(a, b):
+        diff = np.argwhere(a != b)
+        y, x = diff[0]
+        raise AssertionError(f"{len(diff)} pixels differ; first at ({x},{y}): {a[y, x]:08x} vs {b[y, x]:08x}")
+
+
+def test_plain_c1_bit_exact(gpu_ctx_factory, oracle):
+    vol, descs, vox, tf = T.c1_scene()
+    cam = S.axis_camera((64, 64, 64), 512, 512)
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf)
+    fb, samples = gpu_frame(ctx, cam, 512, 512)
+    ref = oracle_frame(oracle, descs, vox, tf, cam, 512, 512)
+    assert_same_fb(fb, ref["fb"])
+    assert samples == ref["samples"]
+    assert (fb != 0).mean() > 0.1
+
+
+def test_partials_depth_bit_exact(gpu_ctx_factory, oracle):
+    vol, descs, vox, tf = T.chopsuey_scene(48, 8)
+    W, H = 72, 56
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8)
+    for cam in T.cameras((48, 48, 48), 3, W, H, seed=21):
+        ctx.set_camera(0, *cam)
+        ctx.resize(0, W, H)
+        imgs = np.zeros((8, H, W, 4), np.float32)
+        depth = np.zeros((8, H, W), np.float32)
+        ctx.render_partials(0, imgs, depth)
+        ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=8, want=("rank_images", "rank_depth"))
+        np.testing.assert_array_equal(imgs, ref["rank_images"])
+        np.testing.assert_array_equal(depth, ref["rank_depth"])
+        assert ctx.stats().samples == ref["samples"]
+
+
+@pytest.mark.parametrize("mode", [abi.COMPOSITE_FP32, abi.COMPOSITE_UBYTE])
+@pytest.mark.parametrize("n_ranks", [1, 2, 3, 8])
+def test_virtual_ranks_bit_exact(gpu_ctx_factory, oracle, mode, n_ranks):
+    vol, descs, vox, tf = T.chopsuey_scene(64, 8)
+    W, H = 100, 76  # not a multiple of the ray tile
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=n_ranks, composite_mode=mode)
+    for cam in T.cameras((64, 64, 64), 3, W, H, seed=n_ranks):
+        fb, samples = gpu_frame(ctx, cam, W, H)
+        ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=n_ranks, composite_mode=mode)
+        assert_same_fb(fb, ref["fb"])
+        assert samples == ref["samples"]
+        assert ctx.composite_order(0) == [int(r) for r in ref["rank_order"]]
+
+
+def test_uneven_bricks_bit_exact(gpu_ctx_factory, oracle):
+    vol, descs, vox, tf = T.uneven_scene(64)
+    W, H = 96, 96
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=12)
+    for cam in T.cameras((64, 64, 64), 4, W, H, seed=9):
+        fb, samples = gpu_frame(ctx, cam, W, H)
+        ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=12)
+        assert_same_fb(fb, ref["fb"])
+        assert samples == ref["samples"]
+
+
+def test_reference_kd_order_mode(gpu_ctx_factory, oracle):
+    vol, descs, vox, tf = T.uneven_scene(48)
+    W, H = 64, 64
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=12, order_mode=abi.ORDER_REFERENCE_KD)
+    for cam in T.cameras((48, 48, 48), 3, W, H, seed=4):
+        fb, _ = gpu_frame(ctx, cam, W, H)
+        ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=12, order_mode=oracle.ORDER_REFERENCE_KD)
+        assert_same_fb(fb, ref["fb"])
+
+
+@pytest.mark.parametrize("kw", [
+    dict(crosshair=1),
+    dict(spp=3),
+    dict(heat_map=1, heat_map_scale=0.01),
+    dict(island_id=1, num_islands=3),
+    dict(jitter_mode=abi.JITTER_NONE),
+    dict(jitter_mode=abi.JITTER_CONST, jitter_value=0.37),
+    dict(dt=2.0),
+    dict(dt=0.25, et_alpha=0.5),
+    dict(accum_id=0, crosshair=1, spp=2, composite_mode=abi.COMPOSITE_UBYTE),
+])
+def test_output_stage_options(gpu_ctx_factory, oracle, kw):
+    vol, descs, vox, tf = T.chopsuey_scene(48, 4)
+    W, H = 80, 64
+    cam = T.cameras((48, 48, 48), 1, W, H, seed=13)[0]
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=4, **kw)
+    fb, samples = gpu_frame(ctx, cam, W, H)
+    ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=4, **kw)
+    assert_same_fb(fb, ref["fb"])
+    assert samples == ref["samples"]
+
+
+def test_progressive_accumulation(gpu_ctx_factory, oracle):
+    vol, descs, vox, tf = T.chopsuey_scene(48, 2)
+    W, H = 64, 48
+    cam = T.cameras((48, 48, 48), 1, W, H, seed=17)[0]
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=2)
+    ctx.set_camera(0, *cam)
+    ctx.resize(0, W, H)
+    acc = np.zeros((2, W * H, 4), np.float32)
+    for k in range(3):
+        ctx.set_params(accum_id=k, accumulate=1)
+        fb = ctx.render(0, width=W, height=H)
+        ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H,
+                            oracle.make_params(accum_id=k, accumulate=1), n_ranks=2, accum=acc)
+        assert_same_fb(fb, ref["fb"])
+
+
+def test_pathological_cameras(gpu_ctx_factory, oracle):
+    vol, descs, vox, tf = T.chopsuey_scene(32, 8)
+    W, H = 40, 40
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8)
+    cams = [
+        S.look_at_camera([16.0, 16.0, 16.0], [40.0, 17.0, 15.0], [0, 1, 0], 60.0, W, H),  # inside, on a face
+        S.look_at_camera([16.3, 5.0, 9.0], [16.3, 5.0, -30.0], [0, 1, 0], 30.0, W, H),   # axis-aligned rays
+        S.look_at_camera([-50.0, 16.0, 16.0], [100.0, 16.0, 16.0], [0, 0, 1], 5.0, W, H),  # along x through faces
+        S.look_at_camera([1e4, 2e3, -3e3], [16.0, 16.0, 16.0], [0, 1, 0], 0.5, W, H),  # far away
+        S.look_at_camera([32.0, 32.0, 32.0], [0.0, 0.0, 0.0], [0, 1, 0], 90.0, W, H),   # on a corner
+    ]
+    for cam in cams:
+        fb, samples = gpu_frame(ctx, cam, W, H)
+        ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=8)
+        assert_same_fb(fb, ref["fb"])
+        assert samples == ref["samples"]
+
+
+@pytest.mark.parametrize("mode", [abi.COMPOSITE_FP32, abi.COMPOSITE_UBYTE])
+def test_partials_then_composite_equals_fused(gpu_ctx_factory, mode):
+    torch = pytest.importorskip("torch")
+    vol, descs, vox, tf = T.chopsuey_scene(64, 8)
+    W, H = 128, 96
+    cam = T.cameras((64, 64, 64), 1, W, H, seed=23)[0]
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8, composite_mode=mode)
+    fused, _ = gpu_frame(ctx, cam, W, H)
+    imgs = torch.zeros((8, H, W, 4), dtype=torch.float32, device="cuda")
+    ctx.render_partials(0, imgs)
+    out = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+    abi.composite_over(imgs, ctx.composite_order(0), W, H, mode, fb=out)
+    torch.cuda.synchronize()
+    assert_same_fb(out.cpu().numpy().view(np.uint32), fused)
+    if mode == abi.COMPOSITE_UBYTE:
+        # the same blend from externally quantised RGBA8 rank images
+        q = (imgs.clamp(0, 1) * 255 + 0.5).to(torch.int32)
+        packed = (q[..., 0] | (q[..., 1] << 8) | (q[..., 2] << 16) | (q[..., 3] << 24)).contiguous()
+        out8 = abi.composite_over_rgba8(packed.cpu().numpy().view(np.uint32), ctx.composite_order(0), W, H)
+        assert_same_fb(out8, fused)
+
+
+def test_batch_equals_single_renders(gpu_ctx_factory):
+    torch = pytest.importorskip("torch")
+    vol, descs, vox, tf = T.uneven_scene(64)
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=12)
+    sizes = [(96, 96), (64, 48), (96, 96), (40, 72), (64, 64)]
+    singles = []
+    for v, (W, H) in enumerate(sizes):
+        cam = S.orbit_cameras((64, 64, 64), len(sizes), W, H, seed=31)[v]
+        ctx.set_camera(v, *cam)
+        ctx.resize(v, W, H)
+        singles.append(ctx.render(v, width=W, height=H))
+    fbs =[torch.zeros((H, W), dtype=torch.int32, device="cuda") for (W, H) in sizes]
+    b = ctx.batch(list(range(len(sizes))), fbs)
+    for cfg in [(16, 8), (8, 8), (32, 4)]:
+        for f in fbs:
+            f.zero_()
+        b.set_config(*cfg)
+        b.launch()
+        torch.cuda.synchronize()
+        for f, s in zip(fbs, singles):
+            assert_same_fb(f.cpu().numpy().view(np.uint32), s)
+    for f in fbs:
+        f.zero_()
+    b.launch_graph()
+    b.launch_graph()
+    torch.cuda.synchronize()
+    for f, s in zip(fbs, singles):
+        assert_same_fb(f.cpu().numpy().view(np.uint32), s)
+    w, h, ms = b.autotune(reps=1)
+    assert (w, h) in [(8, 8), (16, 8), (32, 4)] and ms > 0
+    # a camera change is picked up by the next (graph) launch
+    new_cam = S.orbit_cameras((64, 64, 64), 1, 96, 96, seed=99)[0]
+    ctx.set_camera(0, *new_cam)
+    b.launch_graph()
+    torch.cuda.synchronize()
+    assert_same_fb(fbs[0].cpu().numpy().view(np.uint32), ctx.render(0, width=96, height=96))
+    b.close()
+    # host frame buffers through the convenience entry point
+    host = [np.zeros((H, W), np.uint32) for (W, H) in sizes]
+    ctx.render_batch(list(range(len(sizes))), host)
+    assert_same_fb(host[1], singles[1])
+
+
+def test_device_tensors_as_inputs(gpu_ctx_factory, oracle):
+    torch = pytest.importorskip("torch")
+    vol, descs, vox, tf = T.chopsuey_scene(32, 2)
+    dvox = [torch.from_numpy(v).cuda() for v in vox]
+    dtf = torch.from_numpy(tf).cuda()
+    ctx = setup_ctx(gpu_ctx_factory, descs, dvox, dtf, n_ranks=2)
+    cam = T.cameras((32, 32, 32), 1, 48, 48, seed=2)[0]
+    ctx.set_camera(0, *cam)
+    ctx.resize(0, 48, 48)
+    out = torch.zeros((48, 48), dtype=torch.int32, device="cuda")
+    ctx.render(0, out)
+    torch.cuda.synchronize()
+    ref = oracle_frame(oracle, descs, vox, tf, cam, 48, 48, n_ranks=2)
+    assert_same_fb(out.cpu().numpy().view(np.uint32), ref["fb"])
+
+
+def test_error_paths(gpu_ctx_factory):
+    vol, descs, vox, tf = T.chopsuey_scene(32, 2)
+    ctx = gpu_ctx_factory()
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.render(0, width=8, height=8)
+    assert e.value.code in (abi.ERR_NOT_READY, abi.ERR_OUT_OF_RANGE)
+    ctx.set_bricks(descs, vox)
+    cam = T.cameras((32, 32, 32), 1, 16, 16)[0]
+    ctx.set_camera(0, *cam)
+    ctx.resize(0, 16, 16)
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.render(0, width=16, height=16)  # no transfer function yet
+    assert e.value.code == abi.ERR_NOT_READY
+    ctx.set_transfer_function(tf)
+    ok = ctx.render(0, width=16, height=16)
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.set_camera(0, [float("nan"), 0, 0], cam[1], cam[2], cam[3])
+    assert e.value.code == abi.ERR_INVALID_ARGUMENT
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.set_ranks(5)
+    assert e.value.code == abi.ERR_INVALID_ARGUMENT
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.set_params(dt=0.0)
+    assert e.value.code == abi.ERR_INVALID_ARGUMENT
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.set_params(accum_id=3)
+        ctx.render(0, width=16, height=16)  # no accumulation buffer exists
+    assert e.value.code == abi.ERR_NOT_READY
+    ctx.set_params()
+    # a lost virtual rank: the render fails instead of returning a partial image
+    ctx.drop_brick(1)
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.render(0, width=16, height=16)
+    assert e.value.code == abi.ERR_MISSING_BRICK
+    ctx.update_brick(1, vox[1])
+    np.testing.assert_array_equal(ctx.render(0, width=16, height=16), ok)
+    bad = vox[0].copy()
+    bad[3, 3, 3] = np.inf
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.update_brick(0, bad)
+    assert e.value.code == abi.ERR_INVALID_ARGUMENT
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.set_rank_assignment([0, -1], 2)
+    assert e.value.code == abi.ERR_MISSING_BRICK
+
+
+def test_full_size_rows_bit_exact(gpu_ctx_factory, oracle):
+    """512^3 fp32, 2x2x2 chopSuey bricks, 1024^2: whole frame on the GPU, a
+    spread of rows on the CPU oracle."""
+    n, W, H = 512, 1024, 1024
+    vol = S.blob_field((n, n, n), 64, (32.0, 80.0), seed=2001)
+    descs = oracle.chopsuey_split((n, n, n), 8)
+    vox = S.extract_bricks(vol, descs)
+    tf = S.ramp_tf()
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8)
+    cams = S.orbit_cameras((n, n, n), 2, W, H, seed=2002)
+    for cam in cams:
+        fb, samples = gpu_frame(ctx, cam, W, H)
+        for y0 in (101, 400, 512, 777):
+            ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H, oracle.make_params(), n_ranks=8,
+                                rows=(y0, y0 + 2))
+            assert_same_fb(fb[y0:y0 + 2], ref["fb"][y0:y0 + 2])
+        assert samples > 1e7
