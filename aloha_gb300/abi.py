@@ -32,7 +32,7 @@ EXPORTS = [
     "aloha_set_camera", "aloha_resize", "aloha_get_composite_order", "aloha_render", "aloha_render_partials",
     "aloha_composite_over", "aloha_composite_over_rgba8", "aloha_get_stats", "aloha_batch_create",
     "aloha_batch_set_config", "aloha_batch_get_config", "aloha_batch_launch", "aloha_batch_launch_graph",
-    "aloha_batch_autotune", "aloha_batch_destroy", "aloha_render_batch",
+    "aloha_batch_autotune", "aloha_batch_destroy", "aloha_render_batch", "aloha_forward", "aloha_backward",
 ]
 
 
@@ -96,6 +96,8 @@ _SIGS = {
     "aloha_batch_autotune": ([P, P, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(ctypes.c_float)], I),
     "aloha_batch_destroy": ([P], I),
     "aloha_render_batch": ([P, P, I, ctypes.POINTER(P), P], I),
+    "aloha_forward": ([P, I, P, I, P], I),
+    "aloha_backward": ([P, I, P, P, P, P, P, P], I),
 }
 
 
@@ -255,6 +257,18 @@ class Context:
         v = np.ascontiguousarray(views, dtype=np.int32)
         ptrs = (P * n)(*[_addr(f) for f in fbs])
         self._check(self._lib.aloha_render_batch(self.h, _addr(v), n, ptrs, _stream(stream)))
+
+    def forward(self, view: int, rgba, checkpoint_every: int = 32, stream=None):
+        """Differentiable render of `view` into float RGBA (H, W, 4); keeps checkpoints for backward()."""
+        self._check(self._lib.aloha_forward(self.h, view, _addr(rgba), int(checkpoint_every), _stream(stream)))
+        return rgba
+
+    def backward(self, view: int, dl_drgba, dl_dtf, dl_ddensity, grid_lo, grid_dims, stream=None):
+        """Accumulate dL/dtf and dL/ddensity (on the grid at grid_lo, dims x,y,z) for dL/dRGBA."""
+        lo = np.ascontiguousarray(grid_lo, dtype=np.int32)
+        dims = np.ascontiguousarray(grid_dims, dtype=np.int32)
+        self._check(self._lib.aloha_backward(self.h, view, _addr(dl_drgba), _addr(dl_dtf), _addr(dl_ddensity),
+                                             _addr(lo), _addr(dims), _stream(stream)))
 
     def stats(self) -> Stats:
         s = Stats()

@@ -1,0 +1,85 @@
+"""torch.autograd binding of the differentiable march.
+
+``render_views(renderer, tf, density, views)`` returns float RGBA images
+(views, H, W, 4) that are differentiable with respect to the transfer-function
+table ``tf`` (n, 4) and the density volume ``density`` (nz, ny, nx), both CUDA
+float32 tensors.  The forward stores the march state every K samples; the
+backward replays each K-sample segment from its checkpoint in parallel (see
+csrc/adjoint.cu) and accumulates the gradients.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import abi
+from . import volfile
+
+
+class DifferentiableRenderer:
+    """A context holding one volume split into bricks (one virtual rank)."""
+
+    def __init__(self, dims, bricks: int | list = 1, checkpoint_every: int = 32, device: int = 0, **params):
+        self.dims = [int(d) for d in dims]
+        if isinstance(bricks, int):
+            self.descs = volfile.grid_split(self.dims, ([], [], [])) if bricks == 1 else \
+                volfile.chopsuey_split(self.dims, bricks)
+        else:
+            self.descs = list(bricks)
+        self.k = int(checkpoint_every)
+        self.ctx = abi.Context(device)
+        self._uploaded = False
+        self._params = params
+
+    def _upload(self, tf: torch.Tensor, density: torch.Tensor):
+        vox = [volfile.brick_voxels(density.detach(), d) for d in self.descs]
+        if not self._uploaded:
+            self.ctx.set_bricks(self.descs, vox)
+            self.ctx.set_ranks(1)
+            self.ctx.set_params(**self._params)
+            self._uploaded = True
+        else:
+            for i, v in enumerate(vox):
+                self.ctx.update_brick(i, v)
+        self.ctx.set_transfer_function(tf.detach().contiguous())
+
+    def set_camera(self, view: int, cam, width: int, height: int):
+        self.ctx.set_camera(view, *cam)
+        self.ctx.resize(view, width, height)
+
+    def close(self):
+        self.ctx.close()
+
+
+class _Render(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, tf, density, renderer: DifferentiableRenderer, views, size):
+        if not (tf.is_cuda and density.is_cuda):
+            raise ValueError("tf and density must be CUDA tensors")
+        if tf.dtype != torch.float32 or density.dtype != torch.float32:
+            raise ValueError("tf and density must be float32")
+        W, H = size
+        renderer._upload(tf, density)
+        stream = torch.cuda.current_stream()
+        out = torch.empty((len(views), H, W, 4), dtype=torch.float32, device=density.device)
+        for i, v in enumerate(views):
+            renderer.ctx.forward(v, out[i], renderer.k, stream)
+        ctx.renderer, ctx.views = renderer, list(views)
+        ctx.tf_shape, ctx.density_shape = tf.shape, density.shape
+        return out
+
+    @staticmethod
+    def backward(ctx, grad):
+        r: DifferentiableRenderer = ctx.renderer
+        grad = grad.contiguous().float()
+        dtf = torch.zeros(ctx.tf_shape, dtype=torch.float32, device=grad.device)
+        dden = torch.zeros(ctx.density_shape, dtype=torch.float32, device=grad.device)
+        stream = torch.cuda.current_stream()
+        nz, ny, nx = ctx.density_shape
+        for i, v in enumerate(ctx.views):
+            r.ctx.backward(v, grad[i], dtf, dden, (0, 0, 0), (nx, ny, nz), stream)
+        return dtf, dden, None, None, None
+
+
+def render_views(renderer: DifferentiableRenderer, tf: torch.Tensor, density: torch.Tensor, views, size):
+    """Differentiable render of `views` (each set with renderer.set_camera at `size` = (W, H))."""
+    return _Render.apply(tf, density, renderer, list(views), tuple(size))

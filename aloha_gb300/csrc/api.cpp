@@ -16,6 +16,7 @@
 #include <string>
 #include <vector>
 
+#include "adjoint.h"
 #include "batch_internal.h"
 #include "internal.h"
 #include "order.h"
@@ -24,6 +25,25 @@ using namespace aloha;
 
 namespace {
 
+// Scratch of the differentiable form for one view (checkpoints, final
+// colours, the segment work list).
+struct TrainState {
+  Checkpoint* ckpt = nullptr;
+  float4* final_rgba = nullptr;
+  uint2* work = nullptr;
+  unsigned* work_count = nullptr;
+  int* overflow = nullptr;
+  size_t bytes = 0;
+  unsigned k = 0, cap = 0;
+  size_t npx = 0;
+  bool valid = false;
+  void release() {
+    for (void* p : {(void*)ckpt, (void*)final_rgba, (void*)work, (void*)work_count, (void*)overflow})
+      if (p) cudaFree(p);
+    *this = TrainState();
+  }
+};
+
 struct ViewState {
   bool has_camera = false, has_size = false, dirty = true;
   float org[3], dir_00[3], dir_du[3], dir_dv[3];
@@ -31,6 +51,7 @@ struct ViewState {
   Schedule sched;
   float4* accum = nullptr;  // [n_ranks][H*W]
   size_t accum_elems = 0;
+  TrainState train;
 };
 
 struct DeviceBuffer {
@@ -115,6 +136,11 @@ struct aloha_ctx {
   } while (0)
 
 namespace {
+
+// Any change of scene, parameters or partition invalidates stored checkpoints.
+void invalidate_training(aloha_ctx* c) {
+  for (auto& v : c->views) v.train.valid = false;
+}
 
 // Upload dirty view state (camera, size, schedule) for `view` on `s`.
 int prepare_view(aloha_ctx* c, int view, cudaStream_t s) {
@@ -256,6 +282,7 @@ int set_partition(aloha_ctx* c, int n_ranks) {
   c->brick_rank = br;
   c->tree = tree;
   for (auto& v : c->views) v.dirty = true;
+  invalidate_training(c);
   return ALOHA_OK;
 }
 
@@ -365,8 +392,10 @@ int aloha_destroy(aloha_ctx* c) {
   if (!c) return ALOHA_ERR_NULL_POINTER;
   cudaSetDevice(c->device);
   cudaDeviceSynchronize();
-  for (auto& v : c->views)
+  for (auto& v : c->views) {
     if (v.accum) cudaFree(v.accum);
+    v.train.release();
+  }
   for (DeviceBuffer* b : {&c->voxels, &c->bricks_dev, &c->staging_in, &c->tf, &c->views_dev, &c->sched_dev,
                           &c->counter, &c->flag, &c->staging_out})
     b->release();
@@ -383,6 +412,7 @@ int aloha_set_render_params(aloha_ctx* c, const aloha_render_params* p) {
   if (p->order_mode != c->params.order_mode)
     for (auto& v : c->views) v.dirty = true;
   c->params = *p;
+  invalidate_training(c);
   return ALOHA_OK;
 }
 
@@ -406,6 +436,7 @@ static int upload_brick(aloha_ctx* c, int b, const float* src) {
   CUDA_TRY(c, cudaMemcpy(&bad, c->flag.ptr, sizeof(int), cudaMemcpyDeviceToHost));
   if (bad) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "brick %d holds a non-finite voxel", b);
   c->brick_present[b] = 1;
+  invalidate_training(c);
   return ALOHA_OK;
 }
 
@@ -512,6 +543,7 @@ int aloha_set_transfer_function(aloha_ctx* c, const float* rgba, int n) {
   CUDA_TRY(c, c->tf.ensure(h.size() * sizeof(float)));
   CUDA_TRY(c, cudaMemcpy(c->tf.ptr, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
   c->n_tf = n;
+  invalidate_training(c);
   return ALOHA_OK;
 }
 
@@ -535,6 +567,7 @@ int aloha_set_rank_assignment(aloha_ctx* c, const int* brick_rank, int n_bricks,
   c->brick_rank.assign(brick_rank, brick_rank + n_bricks);
   c->tree.clear();
   for (auto& v : c->views) v.dirty = true;
+  invalidate_training(c);
   return ALOHA_OK;
 }
 
@@ -551,6 +584,7 @@ int aloha_set_camera(aloha_ctx* c, int view, const float* org, const float* dir_
   std::memcpy(v.dir_du, dir_du, 12);
   std::memcpy(v.dir_dv, dir_dv, 12);
   v.has_camera = true;
+  v.train.valid = false;
   v.dirty = true;
   return ALOHA_OK;
 }
@@ -570,6 +604,7 @@ int aloha_resize(aloha_ctx* c, int view, int width, int height) {
   v.width = width;
   v.height = height;
   v.has_size = true;
+  v.train.valid = false;
   v.dirty = true;
   return ALOHA_OK;
 }
@@ -727,6 +762,166 @@ int aloha_composite_over_rgba8(const uint32_t* rank_fbs, const int* order, int n
                                uint32_t* fb, void* stream) {
   const size_t bytes = (size_t)n_ranks * width * height * sizeof(uint32_t);
   return composite_common(rank_fbs, bytes, order, n_ranks, width, height, ALOHA_COMPOSITE_UBYTE, fb, stream, true);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------ differentiable form
+
+namespace {
+
+int check_trainable(aloha_ctx* c) {
+  const aloha_render_params& p = c->params;
+  if (c->n_ranks != 1)
+    return c->fail(ALOHA_ERR_UNSUPPORTED, "the differentiable form needs one virtual rank (aloha_set_ranks(ctx, 1))");
+  if (p.spp != 1 || p.accum_id != 0 || p.accumulate || p.crosshair || p.heat_map || p.num_islands != 1)
+    return c->fail(ALOHA_ERR_UNSUPPORTED,
+                   "the differentiable form needs spp 1, accum_id 0 and no accumulation, crosshair, heat map or islands");
+  return ALOHA_OK;
+}
+
+// Checkpoints per pixel: samples along a ray are at most the chord through
+// the bricks' union / dt plus one per brick (the lattice restarts in every
+// brick), plus slack.
+unsigned checkpoint_capacity(const aloha_ctx* c, unsigned k) {
+  double d2 = 0;
+  for (int a = 0; a < 3; ++a) d2 += (double)(c->bounds_hi[a] - c->bounds_lo[a]) * (c->bounds_hi[a] - c->bounds_lo[a]);
+  const double bound = std::sqrt(d2) / c->params.dt + 2.0 * (double)c->descs.size() + 16.0;
+  return (unsigned)std::ceil(bound / k) + 1;
+}
+
+TrainArgs train_args(aloha_ctx* c, TrainState& t) {
+  const aloha_render_params& p = c->params;
+  TrainArgs a{};
+  a.bricks = static_cast<const DevBrick*>(c->bricks_dev.ptr);
+  a.views = static_cast<const DevView*>(c->views_dev.ptr);
+  a.sched = static_cast<const int*>(c->sched_dev.ptr);
+  a.tf = static_cast<const float4*>(c->tf.ptr);
+  a.n_tf = c->n_tf;
+  a.dt = p.dt;
+  a.et_alpha = p.et_alpha;
+  a.jitter_mode = p.jitter_mode;
+  a.jitter_value = p.jitter_value;
+  a.accum_id = p.accum_id;
+  a.k = t.k;
+  a.ckpt_cap = t.cap;
+  a.ckpt = t.ckpt;
+  a.final_rgba = t.final_rgba;
+  a.work = t.work;
+  a.work_cap = (unsigned)std::min<size_t>(t.npx * t.cap, 0xffffffffu);
+  a.work_count = t.work_count;
+  a.overflow = t.overflow;
+  a.counter = static_cast<unsigned long long*>(c->counter.ptr);
+  return a;
+}
+
+}  // namespace
+
+extern "C" {
+
+int aloha_forward(aloha_ctx* c, int view, float* rgba, int checkpoint_every, void* stream) {
+  if (!c || !rgba) return ALOHA_ERR_NULL_POINTER;
+  if (checkpoint_every < 1 || checkpoint_every > 65535)
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "checkpoint_every %d not in [1, 65535]", checkpoint_every);
+  int rc = check_trainable(c);
+  if (rc) return rc;
+  if ((int)c->descs.size() > 65535) return c->fail(ALOHA_ERR_UNSUPPORTED, "more than 65535 bricks");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  rc = prepare_view(c, view, s);
+  if (rc) return rc;
+  ViewState& v = c->views[view];
+  TrainState& t = v.train;
+  const size_t npx = (size_t)v.width * v.height;
+  const unsigned k = (unsigned)checkpoint_every;
+  const unsigned cap = checkpoint_capacity(c, k);
+  if (npx * cap > 0xffffffffull) return c->fail(ALOHA_ERR_UNSUPPORTED, "too many checkpoint segments for one view");
+  const size_t need = npx * cap * (sizeof(Checkpoint) + sizeof(uint2)) + npx * sizeof(float4);
+  if (t.npx != npx || t.cap != cap) {
+    CUDA_TRY(c, cudaStreamSynchronize(s));
+    t.release();
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(c, cudaMemGetInfo(&free_b, &total_b));
+    if (need > free_b)
+      return c->fail(ALOHA_ERR_OUT_OF_MEMORY, "checkpoints need %zu bytes, %zu free", need, free_b);
+    CUDA_TRY(c, cudaMalloc(&t.ckpt, npx * cap * sizeof(Checkpoint)));
+    CUDA_TRY(c, cudaMalloc(&t.work, npx * cap * sizeof(uint2)));
+    CUDA_TRY(c, cudaMalloc(&t.final_rgba, npx * sizeof(float4)));
+    CUDA_TRY(c, cudaMalloc(&t.work_count, sizeof(unsigned)));
+    CUDA_TRY(c, cudaMalloc(&t.overflow, sizeof(int)));
+    t.npx = npx;
+    t.cap = cap;
+    t.bytes = need;
+  }
+  t.k = k;
+  TrainArgs a = train_args(c, t);
+  const bool host = !is_device_pointer(rgba);
+  a.out_rgba = host ? nullptr : reinterpret_cast<float4*>(rgba);
+  CUDA_TRY(c, cudaMemsetAsync(t.work_count, 0, sizeof(unsigned), s));
+  CUDA_TRY(c, cudaMemsetAsync(t.overflow, 0, sizeof(int), s));
+  CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
+  CUDA_TRY(c, launch_forward_train(a, view, v.width, v.height, s));
+  c->samples_valid = true;
+  t.valid = true;
+  if (host) return finish_host_output(c, rgba, t.final_rgba, npx * sizeof(float4), s);
+  return ALOHA_OK;
+}
+
+int aloha_backward(aloha_ctx* c, int view, const float* dl_drgba, float* dl_dtf, float* dl_ddensity,
+                   const int* grid_lo, const int* grid_dims, void* stream) {
+  if (!c || !dl_drgba || !dl_dtf || !dl_ddensity || !grid_lo || !grid_dims) return ALOHA_ERR_NULL_POINTER;
+  if (view < 0 || view >= (int)c->views.size()) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "view %d", view);
+  int rc = check_trainable(c);
+  if (rc) return rc;
+  ViewState& v = c->views[view];
+  TrainState& t = v.train;
+  if (!t.valid)
+    return c->fail(ALOHA_ERR_NOT_READY, "view %d has no forward checkpoints for the current scene and camera", view);
+  for (int a = 0; a < 3; ++a)
+    if (grid_dims[a] < 1) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "grid dims must be positive");
+  const size_t grid_elems = (size_t)grid_dims[0] * grid_dims[1] * grid_dims[2];
+  std::vector<int4> origin(c->descs.size());
+  for (size_t b = 0; b < c->descs.size(); ++b) {
+    const aloha_brick_desc& d = c->descs[b];
+    for (int a = 0; a < 3; ++a)
+      if (d.voxel_lo[a] < grid_lo[a] || d.voxel_hi[a] > grid_lo[a] + grid_dims[a])
+        return c->fail(ALOHA_ERR_OUT_OF_RANGE, "brick %zu's voxel range leaves the gradient grid", b);
+    origin[b] = make_int4(d.voxel_lo[0] - grid_lo[0], d.voxel_lo[1] - grid_lo[1], d.voxel_lo[2] - grid_lo[2], 0);
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  int overflow = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&overflow, t.overflow, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(c, cudaStreamSynchronize(s));
+  if (overflow) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "a ray needed more checkpoints than reserved");
+  const size_t npx = t.npx, tf_bytes = (size_t)c->n_tf * 4 * sizeof(float), g_bytes = grid_elems * sizeof(float);
+  const bool h_dl = !is_device_pointer(dl_drgba), h_tf = !is_device_pointer(dl_dtf),
+             h_grid = !is_device_pointer(dl_ddensity);
+  // device staging for host arguments, in one block: dL/dRGBA, dL/dtf, dL/ddensity, origins
+  const size_t off_tf = h_dl ? npx * sizeof(float4) : 0;
+  const size_t off_grid = off_tf + (h_tf ? tf_bytes : 0);
+  const size_t off_org = (off_grid + (h_grid ? g_bytes : 0) + 15) & ~(size_t)15;
+  CUDA_TRY(c, c->staging_out.ensure(off_org + origin.size() * sizeof(int4)));
+  char* st = static_cast<char*>(c->staging_out.ptr);
+  TrainArgs a = train_args(c, t);
+  a.dl_drgba = h_dl ? reinterpret_cast<const float4*>(st) : reinterpret_cast<const float4*>(dl_drgba);
+  a.dtf = h_tf ? reinterpret_cast<float*>(st + off_tf) : dl_dtf;
+  a.dgrid = h_grid ? reinterpret_cast<float*>(st + off_grid) : dl_ddensity;
+  a.brick_grid_origin = reinterpret_cast<const int4*>(st + off_org);
+  for (int k = 0; k < 3; ++k) a.grid_dims[k] = grid_dims[k];
+  if (h_dl) CUDA_TRY(c, cudaMemcpyAsync(st, dl_drgba, npx * sizeof(float4), cudaMemcpyHostToDevice, s));
+  if (h_tf) CUDA_TRY(c, cudaMemcpyAsync(a.dtf, dl_dtf, tf_bytes, cudaMemcpyHostToDevice, s));
+  if (h_grid) CUDA_TRY(c, cudaMemcpyAsync(a.dgrid, dl_ddensity, g_bytes, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(c, cudaMemcpyAsync(st + off_org, origin.data(), origin.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  const int per_sm = backward_blocks_per_sm(c->n_tf);
+  if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "backward occupancy query failed");
+  CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
+  CUDA_TRY(c, launch_backward(a, view, c->num_sms * per_sm, s));
+  c->samples_valid = true;
+  if (h_tf) CUDA_TRY(c, cudaMemcpyAsync(dl_dtf, a.dtf, tf_bytes, cudaMemcpyDeviceToHost, s));
+  if (h_grid) CUDA_TRY(c, cudaMemcpyAsync(dl_ddensity, a.dgrid, g_bytes, cudaMemcpyDeviceToHost, s));
+  if (h_dl || h_tf || h_grid) CUDA_TRY(c, cudaStreamSynchronize(s));
+  return ALOHA_OK;
 }
 
 }  // extern "C"

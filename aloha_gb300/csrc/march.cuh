@@ -175,6 +175,25 @@ __device__ __forceinline__ float4 tf_lookup(const float4* __restrict__ tf_s, int
   return make_float4(lerpf(e0.x, e1.x, w), lerpf(e0.y, e1.y, w), lerpf(e0.z, e1.z, w), lerpf(e0.w, e1.w, w));
 }
 
+// Gradient shading .1 + .9 |N.d|, N = g / |g + 1e-4| (deviceCode.cpp:285,294),
+// evaluated as (g.d) / |g + 1e-4|.
+__device__ __forceinline__ float shade_factor(const StencilOut& s, const Ray& r) {
+  const float ex = s.gx + 1e-4f, ey = s.gy + 1e-4f, ez = s.gz + 1e-4f;
+  const float len = sqrtf(fmaf(ez, ez, fmaf(ey, ey, ex * ex)));
+  const float gd = fmaf(s.gz, r.d[2], fmaf(s.gy, r.d[1], s.gx * r.d[0]));
+  return fmaf(0.9f, fabsf(gd / len), 0.1f);
+}
+
+// Front-to-back compositing of one sample (deviceCode.cpp:292-296).
+__device__ __forceinline__ void composite_step(float4& color, const float4 c, float shade) {
+  const float oma = 1.0f - color.w;
+  const float s1 = oma * c.w;
+  color.x = fmaf(s1 * c.x, shade, color.x);
+  color.y = fmaf(s1 * c.y, shade, color.y);
+  color.z = fmaf(s1 * c.z, shade, color.z);
+  color.w = fmaf(oma, c.w, color.w);
+}
+
 // Iteration cap of one brick march: twice the lattice points in [t0, t1) plus
 // 16.  It never binds while t advances by about dt; it ends the loop when
 // t + dt rounds back to t (ray parameters beyond ~2^24 dt).
@@ -200,19 +219,9 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
     const float uy = fmaf(t, r.d[1], r.o[1]) - loy;
     const float uz = fmaf(t, r.d[2], r.o[2]) - loz;
     const StencilOut s = stencil(base, sy, sz, nx, ny, nz, ux, uy, uz);
-    // shading .1 + .9 |N.d|, N = g / |g + 1e-4| (deviceCode.cpp:285,294)
-    const float ex = s.gx + 1e-4f, ey = s.gy + 1e-4f, ez = s.gz + 1e-4f;
-    const float len = sqrtf(fmaf(ez, ez, fmaf(ey, ey, ex * ex)));
-    const float gd = fmaf(s.gz, r.d[2], fmaf(s.gy, r.d[1], s.gx * r.d[0]));
-    const float shade = fmaf(0.9f, fabsf(gd / len), 0.1f);
+    const float shade = shade_factor(s, r);
     const float4 c = tf_lookup(tf_s, n_tf, nf, s.value);
-    // front-to-back compositing (deviceCode.cpp:292-296)
-    const float oma = 1.0f - color.w;
-    const float s1 = oma * c.w;
-    color.x = fmaf(s1 * c.x, shade, color.x);
-    color.y = fmaf(s1 * c.y, shade, color.y);
-    color.z = fmaf(s1 * c.z, shade, color.z);
-    color.w = fmaf(oma, c.w, color.w);
+    composite_step(color, c, shade);
   }
   return n;
 }

@@ -184,6 +184,25 @@ int aloha_batch_destroy(aloha_batch* b);
  * launch and wait for it. */
 int aloha_render_batch(aloha_ctx* ctx, const int* views, int n_items, uint32_t* const* fbs, void* stream);
 
+/* ---- Differentiable form (no reference counterpart).  Needs one virtual
+ * rank (aloha_set_ranks(ctx, 1)), spp 1, accum_id 0, no accumulation,
+ * crosshair, heat map or islands; otherwise ALOHA_ERR_UNSUPPORTED.
+ *
+ * aloha_forward renders `view` into float RGBA (premultiplied, before
+ * quantisation; [height][width][4], host or device), bit-identical to the
+ * frame aloha_render composites, and keeps a checkpoint of the march state
+ * every `checkpoint_every` samples for the view's next aloha_backward. */
+int aloha_forward(aloha_ctx* ctx, int view, float* rgba, int checkpoint_every, void* stream);
+
+/* Gradient of a loss L with respect to the transfer function and the voxel
+ * densities, given dL/dRGBA of the last aloha_forward of `view`
+ * ([height][width][4] float).  Accumulates (+=) into dl_dtf ([n_tf][4]) and
+ * into dl_ddensity, a float grid [dims z][dims y][dims x] whose voxel (0,0,0)
+ * is grid_lo; every brick's voxel range must lie inside it.  Ghost voxels and
+ * clamped edge taps add into the voxel they copy.  Host or device buffers. */
+int aloha_backward(aloha_ctx* ctx, int view, const float* dl_drgba, float* dl_dtf, float* dl_ddensity,
+                   const int* grid_lo, const int* grid_dims, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,46 @@ int render_rows(const Scene* sc, const Schedule* sch, const Camera* cam, int W, 
   return 0;
 }
 
+// Adjoint of the single-rank render: accumulates dL/dtf [n_tf*4] and dL/d
+// density on the grid [dims z][y][x] starting at grid_lo, for dL/dRGBA per
+// pixel.  Returns 0, or -1 on bad arguments.
+template <class R>
+int adjoint_rows(const Scene* sc, const Schedule* sch, const Camera* cam, int W, int H, const Params* p,
+                 const R* dl, R* dtf, R* dgrid, const int* grid_lo, const int* grid_dims, int row_begin, int row_end,
+                 int n_threads, uint64_t* samples) {
+  if (!sc || !sch || !cam || !p || !dl || !dtf || !dgrid || W <= 0 || H <= 0 || sch->n_ranks != 1) return -1;
+  std::vector<BrickView> views(sc->n_bricks);
+  for (int b = 0; b < sc->n_bricks; ++b) {
+    const BrickDesc& d = sc->descs[b];
+    BrickView& v = views[b];
+    v.voxels = sc->voxels[b];
+    for (int a = 0; a < 3; ++a) {
+      v.n[a] = d.voxel_hi[a] - d.voxel_lo[a];
+      v.lo[a] = (float)d.voxel_lo[a];
+      v.space_lo[a] = d.space_lo[a];
+      v.space_hi[a] = d.space_hi[a];
+    }
+  }
+  Grid gr;
+  for (int a = 0; a < 3; ++a) {
+    gr.lo[a] = grid_lo[a];
+    gr.dims[a] = grid_dims[a];
+  }
+  if (row_begin < 0) row_begin = 0;
+  if (row_end > H || row_end < 0) row_end = H;
+  uint64_t total = 0;
+#ifdef _OPENMP
+  if (n_threads <= 0) n_threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(n_threads) reduction(+ : total)
+#endif
+  for (int y = row_begin; y < row_end; ++y)
+    for (int x = 0; x < W; ++x)
+      total += adjoint_pixel<R>(views.data(), sc->tf, sc->n_tf, *sch, *cam, W, x, y, *p, dl + ((size_t)y * W + x) * 4,
+                                dtf, dgrid, gr);
+  if (samples) *samples = total;
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -77,6 +117,13 @@ int ora_render_f32(const Scene* sc, const Schedule* sch, const Camera* cam, int 
 int ora_render_f64(const Scene* sc, const Schedule* sch, const Camera* cam, int W, int H, const Params* p,
                    float max_depth, const Outputs<double>* out, int row_begin, int row_end, int n_threads) {
   return render_rows<double>(sc, sch, cam, W, H, p, max_depth, out, row_begin, row_end, n_threads);
+}
+
+int ora_adjoint_f64(const Scene* sc, const Schedule* sch, const Camera* cam, int W, int H, const Params* p,
+                    const double* dl, double* dtf, double* dgrid, const int* grid_lo, const int* grid_dims,
+                    int row_begin, int row_end, int n_threads, uint64_t* samples) {
+  return adjoint_rows<double>(sc, sch, cam, W, H, p, dl, dtf, dgrid, grid_lo, grid_dims, row_begin, row_end,
+                              n_threads, samples);
 }
 
 // chopSuey split: returns the number of bricks written, or -1.

@@ -36,6 +36,13 @@
 //   * make_rgba rounds to nearest: q = (uint)(clamp(x,0,1)*255 + 0.5).
 // Template parameter R = float gives the parity oracle, R = double the FP64
 // re-render used to state the fp32 error.
+//
+// Parity unpinned: the reference ships no tests, golden images or fixtures,
+// and neither its OptiX build nor its ALOHA_CPU build can be compiled here
+// (owl, fakeOwl, IceT and cuteeOwl are empty submodules; MPI, Qt and OptiX are
+// absent).  The restatement is checked against closed forms derived from the
+// reference's arithmetic (tests/test_oracle.py) and its FP64 adjoint against
+// central differences; tests/golden/ holds regression vectors of this oracle.
 #pragma once
 
 #include <algorithm>
@@ -411,6 +418,177 @@ inline uint64_t render_pixel(const BrickView* bricks, const float* tf, int n_tf,
   }
   if (out.pixel_samples) out.pixel_samples[pixel] = (uint32_t)total;
   return total;
+}
+
+// ---------------------------------------------------------------- adjoint
+//
+// Reverse-mode derivative of one pixel's colour C (front-to-back composite of
+// integrateBrick samples, single virtual rank, spp 1) with respect to the
+// transfer-function table and the voxel densities.  Written as the textbook
+// recursion over stored per-sample states, independent of the GPU's
+// segment-parallel formulation:
+//   rgb' = rgb + (1-a) alpha s c,  a' = a + (1-a) alpha
+//   dL/dalpha = (1-a)(s g.c + gA'),  dL/dc = g (1-a) alpha s,
+//   dL/ds = (1-a) alpha g.c,  gA = gA' (1-alpha) - alpha s g.c
+// with g = dL/drgb (constant along the ray) and gA' the adjoint of alpha after
+// the sample.  Early termination is treated as fixed (no derivative).
+
+struct Grid {
+  int lo[3];
+  int dims[3];
+};
+
+template <class R>
+inline void scatter_voxel(const BrickView& b, int x, int y, int z, R w, R* grid, const Grid& gr) {
+  x = std::min(std::max(x, 0), b.n[0] - 1);
+  y = std::min(std::max(y, 0), b.n[1] - 1);
+  z = std::min(std::max(z, 0), b.n[2] - 1);
+  const int gx = (int)b.lo[0] + x - gr.lo[0], gy = (int)b.lo[1] + y - gr.lo[1], gz = (int)b.lo[2] + z - gr.lo[2];
+  if (gx < 0 || gy < 0 || gz < 0 || gx >= gr.dims[0] || gy >= gr.dims[1] || gz >= gr.dims[2]) return;
+  R* dst = grid + ((size_t)gz * gr.dims[1] + gy) * gr.dims[0] + gx;
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+  *dst += w;
+}
+
+// Scatters w * (trilinear weights at texel coordinate (xb, yb, zb)).
+template <class R>
+inline void scatter_trilinear(const BrickView& b, R xb, R yb, R zb, R w, R* grid, const Grid& gr) {
+  if (w == R(0)) return;
+  const R fx = std::floor(xb), fy = std::floor(yb), fz = std::floor(zb);
+  const R ax = xb - fx, ay = yb - fy, az = zb - fz;
+  const int ix = to_int(fx), iy = to_int(fy), iz = to_int(fz);
+  for (int k = 0; k < 2; ++k)
+    for (int j = 0; j < 2; ++j)
+      for (int i = 0; i < 2; ++i) {
+        const R wt = (i ? ax : R(1) - ax) * (j ? ay : R(1) - ay) * (k ? az : R(1) - az);
+        scatter_voxel(b, ix + i, iy + j, iz + k, w * wt, grid, gr);
+      }
+}
+
+// d(value)/d(voxels) * dv and d(gradient)/d(voxels) . dg for the seven taps.
+template <class R>
+inline void stencil_backward(const BrickView& b, const R u[3], R dv, const R dg[3], R* grid, const Grid& gr) {
+  scatter_trilinear(b, u[0], u[1], u[2], dv, grid, gr);
+  const R h = R(0.5);
+  scatter_trilinear(b, u[0] + h, u[1], u[2], dg[0], grid, gr);
+  scatter_trilinear(b, u[0] - h, u[1], u[2], -dg[0], grid, gr);
+  scatter_trilinear(b, u[0], u[1] + h, u[2], dg[1], grid, gr);
+  scatter_trilinear(b, u[0], u[1] - h, u[2], -dg[1], grid, gr);
+  scatter_trilinear(b, u[0], u[1], u[2] + h, dg[2], grid, gr);
+  scatter_trilinear(b, u[0], u[1], u[2] - h, -dg[2], grid, gr);
+}
+
+// Transfer-function lookup backward: dch = dL/d(r,g,b,alpha) of the lookup.
+template <class R> inline R tf_backward(const float* tf, int n, R v, const R dch[4], R* dtf) {
+  R xb = v * R(n) - R(0.5);
+  R fl = std::floor(xb);
+  R w = xb - fl;
+  int i = to_int(fl);
+  R dv = 0;
+  for (int ch = 0; ch < 4; ++ch) {
+    R e0 = (i >= 0 && i < n) ? R(tf[(size_t)i * 4 + ch]) : R(0);
+    R e1 = (i + 1 >= 0 && i + 1 < n) ? R(tf[(size_t)(i + 1) * 4 + ch]) : R(0);
+    if (i >= 0 && i < n) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+      dtf[(size_t)i * 4 + ch] += (R(1) - w) * dch[ch];
+    }
+    if (i + 1 >= 0 && i + 1 < n) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+      dtf[(size_t)(i + 1) * 4 + ch] += w * dch[ch];
+    }
+    dv += dch[ch] * (e1 - e0) * R(n);
+  }
+  return dv;
+}
+
+// Shading backward: s = .1 + .9 |q|, q = (g.d)/|g + 1e-4|.
+template <class R> inline void shade_backward(const R g[3], const R dir[3], R ds, R dg[3]) {
+  R e[3] = {g[0] + R(1e-4f), g[1] + R(1e-4f), g[2] + R(1e-4f)};
+  R len = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+  R gd = g[0] * dir[0] + g[1] * dir[1] + g[2] * dir[2];
+  R q = gd / len;
+  R sgn = q > 0 ? R(1) : (q < 0 ? R(-1) : R(0));
+  R k = ds * R(0.9f) * sgn;
+  for (int a = 0; a < 3; ++a) dg[a] = k * (dir[a] / len - gd * e[a] / (len * len * len));
+}
+
+struct SampleRec {
+  int brick;
+  double t;
+  double a;  // alpha before the sample
+};
+
+// Adjoint of one pixel; returns the number of samples.
+template <class R>
+inline uint64_t adjoint_pixel(const BrickView* bricks, const float* tf, int n_tf, const Schedule& sch,
+                              const Camera& cam, int W, int x, int y, const Params& p, const R dl[4], R* dtf,
+                              R* dgrid, const Grid& gr) {
+  const int pixel = x + W * y;
+  const R dt = R(p.dt), et = R(p.et_alpha);
+  R org[3], dir[3];
+  generate_ray(cam, x, y, org, dir);
+  std::vector<SampleRec> recs;
+  R color[4] = {0, 0, 0, 0};
+  R tmin = R(0);
+  uint32_t draw = 0;
+  const int r = sch.rank_order[0];
+  for (int j = sch.rank_start[r]; j < sch.rank_start[r + 1]; ++j) {
+    const int bi = sch.rank_bricks[j];
+    const BrickView& b = bricks[bi];
+    R t0, t1;
+    if (!slab(org, dir, b.space_lo, b.space_hi, tmin, R(1e10f), t0, t1)) continue;
+    R ils = R(jitter_value(p, (uint32_t)pixel, draw++));
+    const float span = (float)(t1 - t0) / (float)dt;
+    const uint64_t cap = span < 1e8f ? (uint64_t)(uint32_t)(span * 2.0f) + 16u : 200000016u;
+    uint64_t n = 0;
+    for (R t = first_sample_t(t0, dt, ils); t < t1 && color[3] < et && n < cap; t = t + dt) {
+      ++n;
+      R u[3];
+      for (int a = 0; a < 3; ++a) u[a] = std::fma(t, dir[a], org[a]) - R(b.lo[a]);
+      Stencil<R> s = stencil(b, u);
+      R shade = shade_factor(s.grad, dir);
+      R c[4];
+      tf_lookup(tf, n_tf, s.value, c);
+      recs.push_back(SampleRec{bi, (double)t, (double)color[3]});
+      R oma = R(1) - color[3];
+      R s1 = oma * c[3];
+      color[0] = std::fma(s1 * c[0], shade, color[0]);
+      color[1] = std::fma(s1 * c[1], shade, color[1]);
+      color[2] = std::fma(s1 * c[2], shade, color[2]);
+      color[3] = std::fma(oma, c[3], color[3]);
+    }
+    tmin = t1 + R(1e-20f);
+    if (!(color[3] < et)) break;
+  }
+  R gA = dl[3];
+  for (size_t k = recs.size(); k-- > 0;) {
+    const BrickView& b = bricks[recs[k].brick];
+    const R t = R(recs[k].t), a = R(recs[k].a);
+    R u[3];
+    for (int ax = 0; ax < 3; ++ax) u[ax] = std::fma(t, dir[ax], org[ax]) - R(b.lo[ax]);
+    Stencil<R> s = stencil(b, u);
+    R shade = shade_factor(s.grad, dir);
+    R c[4];
+    tf_lookup(tf, n_tf, s.value, c);
+    const R oma = R(1) - a;
+    const R gc = dl[0] * c[0] + dl[1] * c[1] + dl[2] * c[2];
+    R dch[4];
+    for (int ch = 0; ch < 3; ++ch) dch[ch] = dl[ch] * oma * c[3] * shade;
+    dch[3] = oma * (shade * gc + gA);
+    const R ds = oma * c[3] * gc;
+    gA = gA * (R(1) - c[3]) - c[3] * shade * gc;
+    const R dv = tf_backward(tf, n_tf, s.value, dch, dtf);
+    R dg[3];
+    shade_backward(s.grad, dir, ds, dg);
+    stencil_backward(b, u, dv, dg, dgrid, gr);
+  }
+  return recs.size();
 }
 
 // ---------------------------------------------------------------- layout

@@ -307,6 +307,43 @@ def render(descs, voxels, tf: np.ndarray, camera, W: int, H: int, params: Params
     return res
 
 
+def adjoint(descs, voxels, tf: np.ndarray, camera, W: int, H: int, dl_drgba: np.ndarray,
+            grid_lo, grid_dims, params: Params | None = None, threads: int = 0, sched=None) -> dict:
+    """FP64 adjoint of the single-rank render: dL/dtf (n,4) and dL/ddensity on
+    the grid (dims z,y,x) for dL/dRGBA (H,W,4) of the frame before quantisation."""
+    params = params or make_params()
+    L = lib()
+    if not getattr(L, "_adj_ready", False):
+        L.ora_adjoint_f64.argtypes = [ctypes.POINTER(Scene), ctypes.POINTER(Schedule), ctypes.POINTER(Camera),
+                                      ctypes.c_int, ctypes.c_int, ctypes.POINTER(Params), c_double_p, c_double_p,
+                                      c_double_p, c_int_p, c_int_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_u64_p]
+        L._adj_ready = True
+    nb = len(descs)
+    if sched is None:
+        sched = schedule(descs, 1, list(camera.org))
+    rank_order, rank_start, rank_bricks, _ = sched
+    desc_arr = (BrickDesc * nb)(*[dict_to_desc(d) for d in descs])
+    vox = [np.ascontiguousarray(v, dtype=np.float32) for v in voxels]
+    vptr = (c_float_p * nb)(*[_ptr(v, ctypes.c_float) for v in vox])
+    tf = np.ascontiguousarray(tf, dtype=np.float32)
+    sc = Scene(desc_arr, vptr, nb, _ptr(tf, ctypes.c_float), tf.shape[0])
+    sch = Schedule(1, _ptr(rank_order, ctypes.c_int), _ptr(rank_start, ctypes.c_int), _ptr(rank_bricks, ctypes.c_int))
+    dl = np.ascontiguousarray(dl_drgba, dtype=np.float64).reshape(H, W, 4)
+    dtf = np.zeros((tf.shape[0], 4), np.float64)
+    gd = [int(v) for v in grid_dims]
+    dgrid = np.zeros((gd[2], gd[1], gd[0]), np.float64)
+    glo = np.asarray(grid_lo, dtype=np.int32)
+    gdim = np.asarray(gd, dtype=np.int32)
+    samples = np.zeros(1, np.uint64)
+    rc = L.ora_adjoint_f64(ctypes.byref(sc), ctypes.byref(sch), ctypes.byref(camera), W, H, ctypes.byref(params),
+                           _ptr(dl, ctypes.c_double), _ptr(dtf, ctypes.c_double), _ptr(dgrid, ctypes.c_double),
+                           _ptr(glo, ctypes.c_int), _ptr(gdim, ctypes.c_int), 0, H, threads,
+                           _ptr(samples, ctypes.c_uint64))
+    if rc != 0:
+        raise RuntimeError("oracle adjoint failed (single rank and spp 1 only)")
+    return {"dtf": dtf, "ddensity": dgrid, "samples": int(samples[0])}
+
+
 def jitter_hash(pixel: int, accum_id: int, draw: int) -> float:
     return float(lib().ora_jitter_hash(pixel, accum_id, draw))
 

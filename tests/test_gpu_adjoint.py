@@ -1,0 +1,197 @@
+"""Differentiable form on the GPU: forward parity, gradients against the
+FP64 oracle adjoint and against central finite differences (eps 1e-3)."""
+import numpy as np
+import pytest
+
+from aloha_gb300 import abi
+from aloha_gb300 import scenes as S
+from tests import scenes_for_tests as T
+
+pytestmark = pytest.mark.gpu
+
+
+def setup(make, descs, vox, tf, **params):
+    ctx = make()
+    ctx.set_bricks(descs, vox)
+    ctx.set_transfer_function(tf)
+    ctx.set_ranks(1)
+    ctx.set_params(**params)
+    return ctx
+
+
+def rel_err(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def density_scene(n=64, seed=5, bricks=1):
+    vol = S.blob_field((n, n, n), 12, (n / 16.0, n / 6.0), seed=seed)
+    if bricks == 1:
+        descs = S.single_brick((n, n, n))
+    else:
+        from aloha_gb300 import volfile as V
+        descs = V.chopsuey_split((n, n, n), bricks)
+    return vol, descs, S.extract_bricks(vol, descs)
+
+
+@pytest.mark.parametrize("k", [1, 7, 32])
+def test_forward_is_the_render(gpu_ctx_factory, oracle, k):
+    vol, descs, vox = density_scene(48, bricks=8)
+    tf = S.ramp_tf()
+    W, H = 72, 64
+    ctx = setup(gpu_ctx_factory, descs, vox, tf)
+    cam = T.cameras((48, 48, 48), 1, W, H, seed=3)[0]
+    ctx.set_camera(0, *cam)
+    ctx.resize(0, W, H)
+    img = np.zeros((H, W, 4), np.float32)
+    ctx.forward(0, img, k)
+    samples = ctx.stats().samples
+    ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H, oracle.make_params(), n_ranks=1,
+                        want=("final", "fb"))
+    np.testing.assert_array_equal(img, ref["final"])
+    assert samples == ref["samples"]
+    np.testing.assert_array_equal(ctx.render(0, width=W, height=H), ref["fb"])
+
+
+@pytest.mark.parametrize("bricks,k", [(1, 32), (8, 32), (8, 5)])
+def test_backward_matches_fp64_oracle(gpu_ctx_factory, oracle, bricks, k):
+    n = 48
+    vol, descs, vox = density_scene(n, bricks=bricks)
+    tf = S.ramp_tf()
+    W, H = 80, 80
+    ctx = setup(gpu_ctx_factory, descs, vox, tf)
+    rng = np.random.default_rng(bricks + k)
+    dtf = np.zeros((tf.shape[0], 4), np.float32)
+    dden = np.zeros((n, n, n), np.float32)
+    ref_tf = np.zeros((tf.shape[0], 4))
+    ref_den = np.zeros((n, n, n))
+    for v, cam in enumerate(T.cameras((n, n, n), 2, W, H, seed=7)):
+        ctx.set_camera(v, *cam)
+        ctx.resize(v, W, H)
+        img = np.zeros((H, W, 4), np.float32)
+        ctx.forward(v, img, k)
+        dl = rng.uniform(-1, 1, (H, W, 4)).astype(np.float32)
+        ctx.backward(v, dl, dtf, dden, (0, 0, 0), (n, n, n))
+        r = oracle.adjoint(descs, vox, tf, oracle.make_camera(*cam), W, H, dl, (0, 0, 0), (n, n, n))
+        ref_tf += r["dtf"]
+        ref_den += r["ddensity"]
+    assert rel_err(dtf, ref_tf) < 1e-3
+    assert rel_err(dden, ref_den) < 1e-3
+    assert np.count_nonzero(dden) > 1000
+
+
+def _loss(ctx, views, W, H, weights):
+    total = 0.0
+    for v in views:
+        img = np.zeros((H, W, 4), np.float32)
+        ctx.forward(v, img, 32)
+        total += float((img.astype(np.float64) * weights[v]).sum())
+    return total
+
+
+@pytest.mark.parametrize("et", [0.99, 2.0])
+def test_central_differences(gpu_ctx_factory, et):
+    """dL/dtf and dL/ddensity against (L(x+eps) - L(x-eps)) / 2eps, eps = 1e-3, 64 entries."""
+    n = 32
+    vol, descs, vox = density_scene(n)
+    tf = S.ramp_tf()
+    W = H = 64
+    ctx = setup(gpu_ctx_factory, descs, vox, tf, et_alpha=et)
+    views = [0, 1]
+    for v, cam in zip(views, T.cameras((n, n, n), 2, W, H, seed=11)):
+        ctx.set_camera(v, *cam)
+        ctx.resize(v, W, H)
+    rng = np.random.default_rng(17)
+    weights = {v: rng.uniform(0.5, 1.5, (H, W, 4)) for v in views}
+    dtf = np.zeros((tf.shape[0], 4), np.float32)
+    dden = np.zeros((n, n, n), np.float32)
+    for v in views:
+        img = np.zeros((H, W, 4), np.float32)
+        ctx.forward(v, img, 32)
+        ctx.backward(v, weights[v].astype(np.float32), dtf, dden, (0, 0, 0), (n, n, n))
+    eps = 1e-3
+    errs = []
+    big_tf = np.argwhere(np.abs(dtf) > 0.05 * np.abs(dtf).max())
+    big_den = np.argwhere(np.abs(dden) > 0.05 * np.abs(dden).max())
+    picks = [("tf", tuple(i)) for i in big_tf[rng.choice(len(big_tf), 32, replace=False)]]
+    picks += [("den", tuple(i)) for i in big_den[rng.choice(len(big_den), 32, replace=False)]]
+    for kind, idx in picks:
+        if kind == "tf":
+            f = []
+            for sgn in (1, -1):
+                t2 = tf.copy()
+                t2[idx] += sgn * eps
+                ctx.set_transfer_function(t2)
+                f.append(_loss(ctx, views, W, H, weights))
+            ctx.set_transfer_function(tf)
+            ad = dtf[idx]
+        else:
+            f = []
+            for sgn in (1, -1):
+                v2 = vox[0].copy()
+                v2[idx] += sgn * eps
+                ctx.update_brick(0, v2)
+                f.append(_loss(ctx, views, W, H, weights))
+            ctx.update_brick(0, vox[0])
+            ad = dden[idx]
+        fd = (f[0] - f[1]) / (2 * eps)
+        errs.append(abs(fd - ad) / abs(ad))
+    errs = np.array(errs)
+    # piecewise-linear lookups, the |N.d| kink and (with ET) termination flips
+    # make a few entries non-smooth at this eps
+    assert np.median(errs) < 1e-2
+    assert np.mean(errs < 5e-2) > 0.85
+
+
+def test_autograd_function(gpu_ctx_factory):
+    torch = pytest.importorskip("torch")
+    from aloha_gb300.autograd import DifferentiableRenderer, render_views
+    n, W = 32, 48
+    vol = S.blob_field((n, n, n), 8, (2.0, 5.0), seed=21)
+    r = DifferentiableRenderer((n, n, n), bricks=1, checkpoint_every=16)
+    for v, cam in enumerate(T.cameras((n, n, n), 3, W, W, seed=23)):
+        r.set_camera(v, cam, W, W)
+    tf_t = torch.from_numpy(S.ramp_tf()).cuda().requires_grad_(True)
+    target_tf = torch.from_numpy(S.seeded_tf(5)).cuda()
+    den = torch.from_numpy(vol).cuda().requires_grad_(True)
+    with torch.no_grad():
+        target = render_views(r, target_tf, den, [0, 1, 2], (W, W))
+    img = render_views(r, tf_t, den, [0, 1, 2], (W, W))
+    loss = ((img - target) ** 2).sum()
+    loss.backward()
+    assert tf_t.grad is not None and torch.isfinite(tf_t.grad).all() and tf_t.grad.abs().sum() > 0
+    assert den.grad is not None and torch.isfinite(den.grad).all() and den.grad.abs().sum() > 0
+    # one gradient step on the transfer function lowers the loss
+    with torch.no_grad():
+        tf2 = (tf_t - 1e-3 * tf_t.grad / tf_t.grad.abs().max()).clamp(0, 1)
+        loss2 = ((render_views(r, tf2, den, [0, 1, 2], (W, W)) - target) ** 2).sum()
+    assert float(loss2) < float(loss)
+    r.close()
+
+
+def test_backward_errors(gpu_ctx_factory):
+    vol, descs, vox = density_scene(32, bricks=2)
+    tf = S.ramp_tf()
+    ctx = gpu_ctx_factory()
+    ctx.set_bricks(descs, vox)
+    ctx.set_transfer_function(tf)
+    cam = T.cameras((32, 32, 32), 1, 16, 16)[0]
+    ctx.set_camera(0, *cam)
+    ctx.resize(0, 16, 16)
+    img = np.zeros((16, 16, 4), np.float32)
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.forward(0, img, 32)  # two virtual ranks
+    assert e.value.code == abi.ERR_UNSUPPORTED
+    ctx.set_ranks(1)
+    dtf = np.zeros((256, 4), np.float32)
+    dden = np.zeros((32, 32, 32), np.float32)
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.backward(0, img, dtf, dden, (0, 0, 0), (32, 32, 32))  # no forward yet
+    assert e.value.code == abi.ERR_NOT_READY
+    ctx.forward(0, img, 32)
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.backward(0, img, dtf, dden, (0, 0, 0), (16, 32, 32))  # grid does not cover the bricks
+    assert e.value.code == abi.ERR_OUT_OF_RANGE
+    ctx.set_camera(0, *cam)
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.backward(0, img, dtf, dden, (0, 0, 0), (32, 32, 32))  # camera changed since the forward
+    assert e.value.code == abi.ERR_NOT_READY
