@@ -101,6 +101,12 @@ struct aloha_ctx {
   // transfer function
   DeviceBuffer tf;
   int n_tf = 0;
+  // empty-space macrocells: value range per macrocell (per brick) and the
+  // per-transfer-function empty mask, refreshed before the next render
+  DeviceBuffer mc_ranges, mc_empty, tf_prefix;
+  std::vector<size_t> mc_offset;
+  size_t mc_total = 0;
+  bool empty_dirty = true;
   // virtual ranks
   int n_ranks = 0;
   std::vector<int> brick_rank;
@@ -152,6 +158,12 @@ int prepare_view(aloha_ctx* c, int view, cudaStream_t s) {
   if (!v.has_size) return c->fail(ALOHA_ERR_NOT_READY, "view %d has no size", view);
   for (size_t b = 0; b < c->brick_present.size(); ++b)
     if (!c->brick_present[b]) return c->fail(ALOHA_ERR_MISSING_BRICK, "brick %zu has no data (dropped)", b);
+  if (c->empty_dirty) {
+    CUDA_TRY(c, launch_macrocell_empty(static_cast<const float2*>(c->mc_ranges.ptr), (int)c->mc_total,
+                                       static_cast<const int*>(c->tf_prefix.ptr), c->n_tf,
+                                       static_cast<uint8_t*>(c->mc_empty.ptr), s));
+    c->empty_dirty = false;
+  }
   const int nb = (int)c->descs.size();
   const int stride = 2 * c->n_ranks + 1 + nb;
   if (stride != c->sched_stride) {
@@ -397,7 +409,7 @@ int aloha_destroy(aloha_ctx* c) {
     v.train.release();
   }
   for (DeviceBuffer* b : {&c->voxels, &c->bricks_dev, &c->staging_in, &c->tf, &c->views_dev, &c->sched_dev,
-                          &c->counter, &c->flag, &c->staging_out})
+                          &c->counter, &c->flag, &c->staging_out, &c->mc_ranges, &c->mc_empty, &c->tf_prefix})
     b->release();
   delete c;
   return ALOHA_OK;
@@ -432,7 +444,9 @@ static int upload_brick(aloha_ctx* c, int b, const float* src) {
   CUDA_TRY(c, cudaMemset(c->flag.ptr, 0, sizeof(int)));
   CUDA_TRY(c, launch_pad_brick(dsrc, nx, ny, nz, alloc, db.sy, db.sz / db.sy, nz + 2 * kApron,
                                static_cast<int*>(c->flag.ptr), 0));
-  int bad = 0;
+  CUDA_TRY(c, launch_macrocell_range(db, static_cast<float2*>(c->mc_ranges.ptr) + c->mc_offset[b], 0));
+  c->empty_dirty = true;
+  int bad = 0;  // this copy also waits for the two kernels above
   CUDA_TRY(c, cudaMemcpy(&bad, c->flag.ptr, sizeof(int), cudaMemcpyDeviceToHost));
   if (bad) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "brick %d holds a non-finite voxel", b);
   c->brick_present[b] = 1;
@@ -483,6 +497,18 @@ int aloha_set_bricks(aloha_ctx* c, const aloha_brick_desc* descs, const float* c
   for (int b = 0; b < n; ++b)
     db[b].base = static_cast<const float*>(c->voxels.ptr) + offs[b] + (size_t)kApron * db[b].sz +
                  (size_t)kApron * db[b].sy + kApron;
+  std::vector<size_t> mc_off(n);
+  size_t mc_total = 0;
+  for (int b = 0; b < n; ++b) {
+    mc_off[b] = mc_total;
+    mc_total += (size_t)macrocells(db[b]);
+  }
+  CUDA_TRY(c, c->mc_ranges.ensure(mc_total * sizeof(float2)));
+  CUDA_TRY(c, c->mc_empty.ensure(mc_total));
+  for (int b = 0; b < n; ++b) db[b].empty = static_cast<const uint8_t*>(c->mc_empty.ptr) + mc_off[b];
+  c->mc_offset = mc_off;
+  c->mc_total = mc_total;
+  c->empty_dirty = true;
   c->descs.assign(descs, descs + n);
   c->dev_bricks = db;
   c->brick_offset = offs;
@@ -542,6 +568,12 @@ int aloha_set_transfer_function(aloha_ctx* c, const float* rgba, int n) {
   CUDA_TRY(c, cudaDeviceSynchronize());
   CUDA_TRY(c, c->tf.ensure(h.size() * sizeof(float)));
   CUDA_TRY(c, cudaMemcpy(c->tf.ptr, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+  // prefix counts of entries with non-zero alpha, for the empty-space masks
+  std::vector<int> prefix(n + 1, 0);
+  for (int i = 0; i < n; ++i) prefix[i + 1] = prefix[i] + (h[(size_t)i * 4 + 3] != 0.0f ? 1 : 0);
+  CUDA_TRY(c, c->tf_prefix.ensure(prefix.size() * sizeof(int)));
+  CUDA_TRY(c, cudaMemcpy(c->tf_prefix.ptr, prefix.data(), prefix.size() * sizeof(int), cudaMemcpyHostToDevice));
+  c->empty_dirty = true;
   c->n_tf = n;
   invalidate_training(c);
   return ALOHA_OK;
@@ -681,6 +713,8 @@ int aloha_get_stats(aloha_ctx* c, aloha_stats* out) {
   CUDA_TRY(c, cudaSetDevice(c->device));
   std::memset(out, 0, sizeof *out);
   if (c->samples_valid) {
+    // renders may run on any stream: wait for all of them
+    CUDA_TRY(c, cudaDeviceSynchronize());
     unsigned long long n = 0;
     CUDA_TRY(c, cudaMemcpy(&n, c->counter.ptr, sizeof n, cudaMemcpyDeviceToHost));
     out->samples = n;

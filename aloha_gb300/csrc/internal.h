@@ -15,12 +15,18 @@ constexpr int kApron = 2;
 constexpr int kMaxViews = 4096;
 constexpr int kMaxTF = 2048;  // (n + 4) float4 entries stay under 48 KB of shared memory
 
-// One brick as the kernels see it (64 bytes).
+// Empty-space macrocells: kMacro^3 voxels; a sample whose value-tap cell lies
+// in an empty macrocell has transfer-function alpha exactly 0.
+constexpr int kMacroShift = 3;
+constexpr int kMacro = 1 << kMacroShift;
+
+// One brick as the kernels see it (72 bytes).
 struct DevBrick {
-  const float* base;  // voxel (0,0,0) of the voxel range inside the padded array
-  int sy, sz;         // padded row and slice pitch, in floats
-  int n[3];           // voxel range size
-  float lo[3];        // voxelRange.lower (voxel-unit origin of the brick)
+  const float* base;     // voxel (0,0,0) of the voxel range inside the padded array
+  const uint8_t* empty;  // [mz][my][mx] 1 = every sample there has alpha 0 (null: no skipping)
+  int sy, sz;            // padded row and slice pitch, in floats
+  int n[3];              // voxel range size
+  float lo[3];           // voxelRange.lower (voxel-unit origin of the brick)
   float space_lo[3], space_hi[3];
 };
 
@@ -78,6 +84,13 @@ cudaError_t launch_composite_u8(const uint32_t* imgs, const int* order, int n_ra
 cudaError_t launch_pad_brick(const float* src, int nx, int ny, int nz, float* dst_alloc, int px, int py, int pz,
                              int* nonfinite_flag, cudaStream_t s);
 cudaError_t launch_render_batch(const BatchArgs& a, int tile_w, int tile_h, int grid, cudaStream_t s);
+cudaError_t launch_macrocell_range(const DevBrick& b, float2* out, cudaStream_t s);
+cudaError_t launch_macrocell_empty(const float2* ranges, int count, const int* prefix, int n, uint8_t* empty,
+                                   cudaStream_t s);
+inline int macrocells(const DevBrick& b) {
+  return ((b.n[0] + kMacro - 1) >> kMacroShift) * ((b.n[1] + kMacro - 1) >> kMacroShift) *
+         ((b.n[2] + kMacro - 1) >> kMacroShift);
+}
 // CTAs of the batched kernel that fit on one SM for a tile shape (0 if the shape is unknown).
 int batch_blocks_per_sm(int tile_w, int tile_h, int n_tf);
 

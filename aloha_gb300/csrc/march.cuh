@@ -212,16 +212,40 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
   const float lox = b.lo[0], loy = b.lo[1], loz = b.lo[2];
   const float nf = (float)n_tf;
   const uint32_t cap = march_cap(t0, t1, dt);
+  const uint8_t* __restrict__ empty = b.empty;
+  const int mnx = (nx + kMacro - 1) >> kMacroShift, mny = (ny + kMacro - 1) >> kMacroShift;
   uint32_t n = 0;
-  for (float t = first_sample_t(t0, dt, ils); t < t1 && color.w < et && n < cap; t = t + dt) {
+  float t = first_sample_t(t0, dt, ils);
+  while (t < t1 && color.w < et && n < cap) {
+    float ux = fmaf(t, r.d[0], r.o[0]) - lox;
+    float uy = fmaf(t, r.d[1], r.o[1]) - loy;
+    float uz = fmaf(t, r.d[2], r.o[2]) - loz;
+    if (empty) {
+      // Run through empty space: a sample in an empty macrocell has alpha
+      // exactly 0 and leaves the colour unchanged, so only t and the sample
+      // count advance (the same t += dt sequence as a full sample).
+      bool done = false;
+      while (__ldg(empty + ((min(max((int)floorf(uz), 0), nz - 1) >> kMacroShift) * mny +
+                            (min(max((int)floorf(uy), 0), ny - 1) >> kMacroShift)) * mnx +
+                   (min(max((int)floorf(ux), 0), nx - 1) >> kMacroShift))) {
+        ++n;
+        t = t + dt;
+        if (!(t < t1 && n < cap)) {
+          done = true;
+          break;
+        }
+        ux = fmaf(t, r.d[0], r.o[0]) - lox;
+        uy = fmaf(t, r.d[1], r.o[1]) - loy;
+        uz = fmaf(t, r.d[2], r.o[2]) - loz;
+      }
+      if (done) break;
+    }
     ++n;
-    const float ux = fmaf(t, r.d[0], r.o[0]) - lox;
-    const float uy = fmaf(t, r.d[1], r.o[1]) - loy;
-    const float uz = fmaf(t, r.d[2], r.o[2]) - loz;
     const StencilOut s = stencil(base, sy, sz, nx, ny, nz, ux, uy, uz);
     const float shade = shade_factor(s, r);
     const float4 c = tf_lookup(tf_s, n_tf, nf, s.value);
     composite_step(color, c, shade);
+    t = t + dt;
   }
   return n;
 }

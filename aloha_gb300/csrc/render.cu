@@ -135,7 +135,66 @@ __global__ void pad_brick_kernel(const float* __restrict__ src, int nx, int ny, 
   }
 }
 
+// Value range each macrocell's samples can read: a sample whose value-tap
+// cell is c (c = clamp(floor(u), 0, n-1)) reads voxels c and c+1 (clamped), so
+// macrocell m covers voxels [m*kMacro, m*kMacro + kMacro] per axis.
+__global__ void macrocell_range_kernel(const float* __restrict__ base, int sy, int sz, int nx, int ny, int nz,
+                                       int mnx, int mny, int mnz, float2* __restrict__ out) {
+  const int total = mnx * mny * mnz;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int mx = i % mnx, my = (i / mnx) % mny, mz = i / (mnx * mny);
+    const int x0 = mx * kMacro, y0 = my * kMacro, z0 = mz * kMacro;
+    const int x1 = min(x0 + kMacro, nx - 1), y1 = min(y0 + kMacro, ny - 1), z1 = min(z0 + kMacro, nz - 1);
+    float lo = __int_as_float(0x7f800000), hi = -lo;
+    for (int z = z0; z <= z1; ++z)
+      for (int y = y0; y <= y1; ++y) {
+        const float* row = base + (size_t)z * sz + (size_t)y * sy;
+        for (int x = x0; x <= x1; ++x) {
+          const float v = __ldg(row + x);
+          lo = fminf(lo, v);
+          hi = fmaxf(hi, v);
+        }
+      }
+    out[i] = make_float2(lo, hi);
+  }
+}
+
+// A macrocell is empty when every transfer-function entry its lookups can
+// touch has alpha 0: indices floor(v*n - 1/2) and +1 for v in [lo, hi], with
+// one index of margin on each side for rounding of the interpolated value.
+// prefix[k] = number of entries below k with non-zero alpha.
+__global__ void macrocell_empty_kernel(const float2* __restrict__ ranges, int count, const int* __restrict__ prefix,
+                                       int n, uint8_t* __restrict__ empty) {
+  const float nf = (float)n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    const float2 r = ranges[i];
+    const float xl = fminf(fmaxf(r.x * nf - 0.5f, -8.0f), nf + 8.0f);
+    const float xh = fminf(fmaxf(r.y * nf - 0.5f, -8.0f), nf + 8.0f);
+    const int lo = max((int)floorf(xl) - 1, 0);
+    const int hi = min((int)floorf(xh) + 2, n - 1);
+    const int nonzero = lo <= hi ? __ldg(prefix + hi + 1) - __ldg(prefix + lo) : 0;
+    empty[i] = nonzero == 0 ? 1 : 0;
+  }
+}
+
 static size_t tf_smem(int n_tf) { return (size_t)(n_tf + 4) * sizeof(float4); }
+
+cudaError_t launch_macrocell_range(const DevBrick& b, float2* out, cudaStream_t s) {
+  const int mnx = (b.n[0] + kMacro - 1) >> kMacroShift, mny = (b.n[1] + kMacro - 1) >> kMacroShift,
+            mnz = (b.n[2] + kMacro - 1) >> kMacroShift;
+  const int total = mnx * mny * mnz;
+  const int grid = total < 256 ? 1 : min((total + 127) / 128, 152 * 32);
+  macrocell_range_kernel<<<grid, 128, 0, s>>>(b.base, b.sy, b.sz, b.n[0], b.n[1], b.n[2], mnx, mny, mnz, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_macrocell_empty(const float2* ranges, int count, const int* prefix, int n, uint8_t* empty,
+                                   cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  const int grid = min((count + 255) / 256, 152 * 16);
+  macrocell_empty_kernel<<<grid, 256, 0, s>>>(ranges, count, prefix, n, empty);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_render(const FrameArgs& a, int view, int width, int height, cudaStream_t s) {
   constexpr int TW = 16, TH = 8;

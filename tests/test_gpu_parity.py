@@ -288,6 +288,41 @@ def test_error_paths(gpu_ctx_factory):
     assert e.value.code == abi.ERR_MISSING_BRICK
 
 
+def _band_tf(lo, hi, n=256, alpha=0.5):
+    x = (np.arange(n) + 0.5) / n
+    tf = S.ramp_tf(n).copy()
+    tf[:, 3] = np.where((x >= lo) & (x <= hi), alpha, 0.0)
+    return np.ascontiguousarray(tf, np.float32)
+
+
+def test_empty_space_skipping_is_exact(gpu_ctx_factory, oracle):
+    """Samples in macrocells whose transfer-function alpha is 0 are skipped on
+    the GPU; frames and sample counts must not change."""
+    vol, descs, vox, tf = T.chopsuey_scene(64, 8)
+    W, H = 96, 80
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8)
+    cams = T.cameras((64, 64, 64), 2, W, H, seed=51)
+    tfs = [_band_tf(0.5, 0.53), _band_tf(0.0, 0.01), _band_tf(0.99, 1.0), np.zeros((256, 4), np.float32),
+           _band_tf(0.0, 1.0, alpha=0.05), _band_tf(0.3, 0.3001, n=64), tf]
+    for t in tfs:
+        ctx.set_transfer_function(t)  # masks are rebuilt before the next render
+        for cam in cams:
+            fb, samples = gpu_frame(ctx, cam, W, H)
+            ref = oracle_frame(oracle, descs, vox, t, cam, W, H, n_ranks=8)
+            assert_same_fb(fb, ref["fb"])
+            assert samples == ref["samples"]
+    # a brick update rebuilds its value ranges too
+    bumped = vox[3] + np.float32(0.4)
+    ctx.update_brick(3, bumped)
+    vox2 = list(vox)
+    vox2[3] = bumped
+    for cam in cams:
+        fb, samples = gpu_frame(ctx, cam, W, H)
+        ref = oracle_frame(oracle, descs, vox2, tf, cam, W, H, n_ranks=8)
+        assert_same_fb(fb, ref["fb"])
+        assert samples == ref["samples"]
+
+
 def test_full_size_rows_bit_exact(gpu_ctx_factory, oracle):
     """512^3 fp32, 2x2x2 chopSuey bricks, 1024^2: whole frame on the GPU, a
     spread of rows on the CPU oracle."""
