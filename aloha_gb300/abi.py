@@ -33,6 +33,7 @@ EXPORTS = [
     "aloha_composite_over", "aloha_composite_over_rgba8", "aloha_get_stats", "aloha_batch_create",
     "aloha_batch_set_config", "aloha_batch_get_config", "aloha_batch_launch", "aloha_batch_launch_graph",
     "aloha_batch_autotune", "aloha_batch_destroy", "aloha_render_batch", "aloha_forward", "aloha_backward",
+    "aloha_set_render_tile",
 ]
 
 
@@ -98,6 +99,7 @@ _SIGS = {
     "aloha_render_batch": ([P, P, I, ctypes.POINTER(P), P], I),
     "aloha_forward": ([P, I, P, I, P], I),
     "aloha_backward": ([P, I, P, P, P, P, P, P], I),
+    "aloha_set_render_tile": ([P, I, I], I),
 }
 
 
@@ -238,6 +240,9 @@ class Context:
         return [int(v) for v in buf[:n.value]]
 
     # ---- render
+    def set_render_tile(self, tile_w: int, tile_h: int):
+        self._check(self._lib.aloha_set_render_tile(self.h, int(tile_w), int(tile_h)))
+
     def render(self, view: int, fb=None, stream=None, width: int | None = None, height: int | None = None):
         """Render into `fb` (uint32 W*H, numpy or torch); allocates a numpy buffer if None."""
         if fb is None:

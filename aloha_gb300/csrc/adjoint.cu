@@ -22,6 +22,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <climits>
+
 #include "adjoint.h"
 #include "march.cuh"
 
@@ -43,14 +45,20 @@ __device__ __forceinline__ const int* rank_bricks(const TrainArgs& a, const DevV
 // samples already taken there).  Calls `visit` before compositing each
 // sample; stops after max_samples.  The walk, jitter draws and sample
 // arithmetic are those of render_pixel / march_brick.
-template <class Visit>
+//
+// With SKIP, samples in empty macrocells (transfer-function alpha exactly 0,
+// see march_brick) are not evaluated: `skipped` is called for each of them
+// instead of `visit`, with the unchanged colour.  The backward replay cannot
+// skip: a zero-alpha sample still carries a gradient for the alpha entries.
+template <bool SKIP, class Visit, class Skipped>
 __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevView& v, const float4* tf_s,
                                                  const Ray& ray, uint32_t pixel, Walk w, float t_resume,
                                                  uint32_t nb0, bool resume, float4& color, uint32_t max_samples,
-                                                 Visit visit) {
+                                                 Visit visit, Skipped skipped) {
   const int* __restrict__ rb = rank_bricks(a, v);
   const int j1 = __ldg(a.sched + v.sched + 2);
   const float nf = (float)a.n_tf;
+  const float dt = a.dt;
   uint32_t n = 0;
   for (; w.j < j1; ++w.j) {
     const DevBrick b = a.bricks[__ldg(rb + w.j)];
@@ -64,14 +72,39 @@ __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevVi
       resume = false;
     } else {
       const float ils = jitter(a.jitter_mode, a.jitter_value, pixel, (uint32_t)a.accum_id, w.draw++);
-      t = first_sample_t(t0, a.dt, ils);
+      t = first_sample_t(t0, dt, ils);
     }
-    const uint32_t cap = march_cap(t0, t1, a.dt);
-    for (; t < t1 && color.w < a.et_alpha && nb < cap; t = t + a.dt) {
+    const uint32_t cap = march_cap(t0, t1, dt);
+    const int mnx = (b.n[0] + kMacro - 1) >> kMacroShift, mny = (b.n[1] + kMacro - 1) >> kMacroShift;
+    const float mag = fmaxf(fmaxf(fabsf(ray.o[0]) + fabsf(b.lo[0]), fabsf(ray.o[1]) + fabsf(b.lo[1])),
+                            fabsf(ray.o[2]) + fabsf(b.lo[2])) + fabsf(t1);
+    const float eps = 2e-6f * mag + 1e-4f;
+    while (t < t1 && color.w < a.et_alpha && nb < cap) {
       if (n == max_samples) return n;
       const float ux = fmaf(t, ray.d[0], ray.o[0]) - b.lo[0];
       const float uy = fmaf(t, ray.d[1], ray.o[1]) - b.lo[1];
       const float uz = fmaf(t, ray.d[2], ray.o[2]) - b.lo[2];
+      if (SKIP && b.empty) {
+        const int mx = min(max((int)floorf(ux), 0), b.n[0] - 1) >> kMacroShift;
+        const int my = min(max((int)floorf(uy), 0), b.n[1] - 1) >> kMacroShift;
+        const int mz = min(max((int)floorf(uz), 0), b.n[2] - 1) >> kMacroShift;
+        if (__ldg(b.empty + (mz * mny + my) * mnx + mx)) {
+          const float bnd[3] = {(float)(mx << kMacroShift), (float)(my << kMacroShift), (float)(mz << kMacroShift)};
+          float tb = t1;
+#pragma unroll
+          for (int ax = 0; ax < 3; ++ax) {
+            const float face = ray.d[ax] > 0.f ? bnd[ax] + (float)kMacro - eps : bnd[ax] + eps;
+            tb = fminf(tb, (face - (ray.o[ax] - b.lo[ax])) * (1.0f / ray.d[ax]));
+          }
+          do {
+            skipped(t, w, nb, color);
+            ++n;
+            ++nb;
+            t = t + dt;
+          } while (t < tb && nb < cap && n != max_samples);
+          continue;
+        }
+      }
       const StencilOut s = stencil(b.base, b.sy, b.sz, b.n[0], b.n[1], b.n[2], ux, uy, uz);
       const float shade = shade_factor(s, ray);
       const float4 c = tf_lookup(tf_s, a.n_tf, nf, s.value);
@@ -79,6 +112,7 @@ __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevVi
       composite_step(color, c, shade);
       ++n;
       ++nb;
+      t = t + dt;
     }
     w.tmin = t1 + 1e-20f;
     if (!(color.w < a.et_alpha)) break;
@@ -86,15 +120,11 @@ __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevVi
   return n;
 }
 
-template <int TW, int TH>
-__global__ void __launch_bounds__(TW* TH) forward_train_kernel(TrainArgs a, int view) {
-  extern __shared__ float4 tf_s[];
-  load_tf(tf_s, a.tf, a.n_tf);
-  __syncthreads();
-  const DevView v = a.views[view];
-  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int x = blockIdx.x * TW + (wi % (TW / 8)) * 8 + (lane & 7);
-  const int y = blockIdx.y * TH + (wi / (TW / 8)) * 4 + (lane >> 3);
+// Training forward of one warp's 8 x 4 pixels at (x, y): march, checkpoints,
+// final colour, and the warp-aggregated append of (pixel, segment) items.
+// Returns the lane's sample count.
+__device__ __forceinline__ uint32_t train_subtile(const TrainArgs& a, const DevView& v, const float4* tf_s, int x,
+                                                  int y, int lane) {
   const bool active = x < v.width && y < v.height;
   uint32_t n = 0, nseg = 0;
   uint32_t pixel = 0;
@@ -105,28 +135,33 @@ __global__ void __launch_bounds__(TW* TH) forward_train_kernel(TrainArgs a, int 
     Checkpoint* ck = a.ckpt + (size_t)pixel * a.ckpt_cap;
     const uint32_t K = a.k, cap = a.ckpt_cap;
     uint32_t idx = 0;
-    n = walk_samples(a, v, tf_s, ray, pixel, Walk{0, 0.0f, 0u}, 0.f, 0u, false, color, 0xffffffffu,
-                     [&](const DevBrick&, float t, const Walk& w, uint32_t nb, float, float, float,
-                         const StencilOut&, float, const float4&, const float4& col) {
-                       if (idx % K == 0) {
-                         const uint32_t m = idx / K;
-                         if (m < cap) {
-                           Checkpoint c;
-                           c.r = col.x;
-                           c.g = col.y;
-                           c.b = col.z;
-                           c.a = col.w;
-                           c.t = t;
-                           c.tmin = w.tmin;
-                           c.jd = (uint32_t)w.j | (w.draw << 16);
-                           c.nb = nb;
-                           ck[m] = c;
-                         } else {
-                           atomicOr(a.overflow, 1);
-                         }
-                       }
-                       ++idx;
-                     });
+    // checkpoint before every K-th sample, evaluated or skipped
+    auto checkpoint = [&](float t, const Walk& w, uint32_t nb, const float4& col) {
+      if (idx % K == 0) {
+        const uint32_t m = idx / K;
+        if (m < cap) {
+          Checkpoint c;
+          c.r = col.x;
+          c.g = col.y;
+          c.b = col.z;
+          c.a = col.w;
+          c.t = t;
+          c.tmin = w.tmin;
+          c.jd = (uint32_t)w.j | (w.draw << 16);
+          c.nb = nb;
+          ck[m] = c;
+        } else {
+          atomicOr(a.overflow, 1);
+        }
+      }
+      ++idx;
+    };
+    n = walk_samples<true>(a, v, tf_s, ray, pixel, Walk{0, 0.0f, 0u}, 0.f, 0u, false, color, 0xffffffffu,
+                           [&](const DevBrick&, float t, const Walk& w, uint32_t nb, float, float, float,
+                               const StencilOut&, float, const float4&, const float4& col) {
+                             checkpoint(t, w, nb, col);
+                           },
+                           checkpoint);
     a.final_rgba[pixel] = color;
     if (a.out_rgba) a.out_rgba[pixel] = color;
     nseg = min((n + K - 1) / K, cap);
@@ -148,6 +183,29 @@ __global__ void __launch_bounds__(TW* TH) forward_train_kernel(TrainArgs a, int 
     }
     off += __popc(mask);
   }
+  return n;
+}
+
+// Persistent training forward: warps pull 8 x 4 chunks centre-out (as the
+// render does) from the counter at work_count[1].
+__global__ void __launch_bounds__(128) forward_train_kernel(TrainArgs a, int view) {
+  extern __shared__ float4 tf_s[];
+  load_tf(tf_s, a.tf, a.n_tf);
+  __syncthreads();
+  const DevView v = a.views[view];
+  const int lane = threadIdx.x & 31;
+  const int cxn = (v.width + 7) / 8, cyn = (v.height + 3) / 4;
+  const int total = ring_slots(v.width, v.height, 8, 4);
+  uint32_t n = 0;
+  for (;;) {
+    int chunk = 0;
+    if (lane == 0) chunk = (int)atomicAdd(a.work_count + 1, 1u);
+    chunk = __shfl_sync(0xffffffffu, chunk, 0);
+    if (chunk >= total) break;
+    int ccx, ccy;
+    if (!ring_chunk(chunk, cxn, cyn, ccx, ccy)) continue;
+    n += train_subtile(a, v, tf_s, ccx * 8 + (lane & 7), ccy * 4 + (lane >> 3), lane);
+  }
   count_samples(a.counter, n);
 }
 
@@ -155,10 +213,42 @@ __device__ __forceinline__ void red_add(float* p, float v) {
   if (v != 0.f) atomicAdd(p, v);
 }
 
+// Adds weights of brick voxels (x..x+2, y, z) (y, z already clamped to the
+// brick) into the quad gradient: one float4 atomic when the three voxels are
+// inside the brick, else one scalar atomic per clamped voxel.
+__device__ __forceinline__ void scatter3(const TrainArgs& a, const DevBrick& b, const int4 org, int x, int y, int z,
+                                         float w0, float w1, float w2) {
+  if (w0 == 0.f && w1 == 0.f && w2 == 0.f) return;
+  float4* row = a.dgrid4 + ((size_t)(z + org.z) * a.grid_dims[1] + (size_t)(y + org.y)) * a.grid_dims[0] + org.x;
+  if (x >= 0 && x + 2 < b.n[0]) {
+    atomicAdd(row + x, make_float4(w0, w1, w2, 0.f));
+  } else {
+    const int hi = b.n[0] - 1;
+    red_add(&row[min(max(x, 0), hi)].x, w0);
+    red_add(&row[min(max(x + 1, 0), hi)].x, w1);
+    red_add(&row[min(max(x + 2, 0), hi)].x, w2);
+  }
+}
+
+// The same for voxels (x, x+1): one float2 atomic on the quad's first half.
+__device__ __forceinline__ void scatter2(const TrainArgs& a, const DevBrick& b, const int4 org, int x, int y, int z,
+                                         float w0, float w1) {
+  if (w0 == 0.f && w1 == 0.f) return;
+  float4* row = a.dgrid4 + ((size_t)(z + org.z) * a.grid_dims[1] + (size_t)(y + org.y)) * a.grid_dims[0] + org.x;
+  if (x >= 0 && x + 1 < b.n[0]) {
+    atomicAdd(reinterpret_cast<float2*>(row + x), make_float2(w0, w1));
+  } else {
+    const int hi = b.n[0] - 1;
+    red_add(&row[min(max(x, 0), hi)].x, w0);
+    red_add(&row[min(max(x + 1, 0), hi)].x, w1);
+  }
+}
+
 // Density-gradient scatter of one sample: the 20 voxels of the stencil with
-// their combined weights (value tap and the six gradient taps).  Indices are
-// clamped to the brick (the derivative of clamp addressing) and mapped to the
-// caller's grid, so ghost and apron copies accumulate into the shared voxel.
+// their combined weights (value tap and the six gradient taps), as 4 row
+// quads and 4 row pairs.  Indices are clamped to the brick (the derivative of
+// clamp addressing) and mapped to the caller's grid, so ghost and apron copies
+// accumulate into the voxel they copy.
 __device__ __forceinline__ void stencil_backward(const DevBrick& b, const TrainArgs& a, int brick, float ux,
                                                  float uy, float uz, float dv, float dgx, float dgy, float dgz) {
   const float mx = ux - 0.5f, my = uy - 0.5f, mz = uz - 0.5f;
@@ -174,14 +264,7 @@ __device__ __forceinline__ void stencil_backward(const DevBrick& b, const TrainA
   const int cy = min(max((int)fcy, -kApron), b.n[1]);
   const int cz = min(max((int)fcz, -kApron), b.n[2]);
   const int4 org = a.brick_grid_origin[brick];
-  const size_t sx = (size_t)a.grid_dims[0], sxy = sx * (size_t)a.grid_dims[1];
-  float* __restrict__ G = a.dgrid;
-  auto at = [&](int x, int y, int z) -> float* {
-    x = min(max(x, 0), b.n[0] - 1) + org.x;
-    y = min(max(y, 0), b.n[1] - 1) + org.y;
-    z = min(max(z, 0), b.n[2] - 1) + org.z;
-    return G + ((size_t)z * sxy + (size_t)y * sx + (size_t)x);
-  };
+  const int ny1 = b.n[1] - 1, nz1 = b.n[2] - 1;
   const float wx[2] = {1.f - gx, gx}, wy[2] = {1.f - gy, gy}, wz[2] = {1.f - gz, gz};
   const float wxg[3] = {-(1.f - fx), (1.f - fx) - fx, fx};
   const float wyg[3] = {-(1.f - fy), (1.f - fy) - fy, fy};
@@ -194,20 +277,46 @@ __device__ __forceinline__ void stencil_backward(const DevBrick& b, const TrainA
     for (int j = 0; j < 2; ++j) {
       const float wyz = wy[j] * wz[l];
       const float side = dgy * wyg[myc + j] * wz[l] + dgz * wzg[mzc + l] * wy[j];
+      float w[3];
 #pragma unroll
-      for (int k = 0; k < 3; ++k)
-        red_add(at(ix + k, cy + j, cz + l), wyz * (dgx * wxg[k] + dv * wv[k]) + wv[k] * side);
+      for (int k = 0; k < 3; ++k) w[k] = wyz * (dgx * wxg[k] + dv * wv[k]) + wv[k] * side;
+      scatter3(a, b, org, ix, min(max(cy + j, 0), ny1), min(max(cz + l, 0), nz1), w[0], w[1], w[2]);
     }
-  const int ye = hy ? iy : iy + 2, ze = hz ? iz : iz + 2;
+  const int ye = min(max(hy ? iy : iy + 2, 0), ny1), ze = min(max(hz ? iz : iz + 2, 0), nz1);
   const float wye = dgy * wyg[hy ? 0 : 2], wze = dgz * wzg[hz ? 0 : 2];
 #pragma unroll
   for (int l = 0; l < 2; ++l)
-#pragma unroll
-    for (int i = 0; i < 2; ++i) red_add(at(cx + i, ye, cz + l), wye * wx[i] * wz[l]);
+    scatter2(a, b, org, cx, ye, min(max(cz + l, 0), nz1), wye * wx[0] * wz[l], wye * wx[1] * wz[l]);
 #pragma unroll
   for (int j = 0; j < 2; ++j)
+    scatter2(a, b, org, cx, min(max(cy + j, 0), ny1), ze, wze * wx[0] * wy[j], wze * wx[1] * wy[j]);
+}
+
+// out[v] += q[v].x + q[v-1].y + q[v-2].z along x (each voxel written by one thread).
+__global__ void fold_quads_kernel(const float4* __restrict__ q, float* __restrict__ out, int dx, size_t total) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % (size_t)dx);
+    float s = q[i].x;
+    if (x >= 1) s += q[i - 1].y;
+    if (x >= 2) s += q[i - 2].z;
+    if (s != 0.f) out[i] += s;
+  }
+}
+
+// Adds a pending transfer-function gradient (entries i and i+1, four
+// channels each) to the CTA's shared copy and clears it.
+__device__ __forceinline__ void flush_tf(float* dtf_s, int n, int i, float pend[8]) {
 #pragma unroll
-    for (int i = 0; i < 2; ++i) red_add(at(cx + i, cy + j, ze), wze * wx[i] * wy[j]);
+  for (int k = 0; k < 2; ++k) {
+    const int e = i + k;
+    if (e >= 0 && e < n) {
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch)
+        if (pend[4 * k + ch] != 0.f) atomicAdd(dtf_s + e * 4 + ch, pend[4 * k + ch]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) pend[k] = 0.f;
 }
 
 __global__ void __launch_bounds__(128) backward_kernel(TrainArgs a, int view) {
@@ -233,7 +342,11 @@ __global__ void __launch_bounds__(128) backward_kernel(TrainArgs a, int view) {
     const float gfin = g.w * (1.0f - F.w);
     float4 color = make_float4(ck.r, ck.g, ck.b, ck.a);
     const Walk w0{(int)(ck.jd & 0xffffu), ck.tmin, ck.jd >> 16};
-    nsamp += walk_samples(
+    // transfer-function gradient of consecutive samples with the same lookup
+    // index is summed in registers and added to shared memory once per index
+    int pend_i = INT_MIN;
+    float pend[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    nsamp += walk_samples<false>(
         a, v, tf_s, ray, pixel, w0, ck.t, ck.nb, true, color, a.k,
         [&](const DevBrick& b, float, const Walk& wcur, uint32_t, float ux, float uy, float uz, const StencilOut& s,
             float shade, const float4& c, const float4& col) {
@@ -256,9 +369,14 @@ __global__ void __launch_bounds__(128) backward_kernel(TrainArgs a, int view) {
           const float de[4] = {e1.x - e0.x, e1.y - e0.y, e1.z - e0.z, e1.w - e0.w};
           float dv = 0.f;
 #pragma unroll
+          if (i0 != pend_i) {
+            flush_tf(dtf_s, a.n_tf, pend_i, pend);
+            pend_i = i0;
+          }
+#pragma unroll
           for (int ch = 0; ch < 4; ++ch) {
-            if (i0 >= 0 && i0 < a.n_tf) atomicAdd(dtf_s + i0 * 4 + ch, (1.f - wt) * dch[ch]);
-            if (i0 + 1 >= 0 && i0 + 1 < a.n_tf) atomicAdd(dtf_s + (i0 + 1) * 4 + ch, wt * dch[ch]);
+            pend[ch] += (1.f - wt) * dch[ch];
+            pend[4 + ch] += wt * dch[ch];
             dv += dch[ch] * de[ch] * nf;
           }
           // shading backward: s = .1 + .9 |q|, q = (g.d)/|g + 1e-4|
@@ -271,7 +389,9 @@ __global__ void __launch_bounds__(128) backward_kernel(TrainArgs a, int view) {
           const float inv = 1.0f / len, c3 = gd / (len2 * len);
           stencil_backward(b, a, __ldg(rb + wcur.j), ux, uy, uz, dv, kk * (ray.d[0] * inv - c3 * ex),
                            kk * (ray.d[1] * inv - c3 * ey), kk * (ray.d[2] * inv - c3 * ez));
-        });
+        },
+        [](float, const Walk&, uint32_t, const float4&) {});
+    flush_tf(dtf_s, a.n_tf, pend_i, pend);
   }
   count_samples(a.counter, nsamp);
   __syncthreads();
@@ -282,11 +402,23 @@ size_t backward_smem(int n_tf) { return (size_t)(n_tf + 4) * sizeof(float4) + (s
 
 }  // namespace
 
-cudaError_t launch_forward_train(const TrainArgs& a, int view, int width, int height, cudaStream_t s) {
-  constexpr int TW = 16, TH = 8;
-  dim3 grid((width + TW - 1) / TW, (height + TH - 1) / TH);
-  forward_train_kernel<TW, TH><<<grid, TW * TH, (size_t)(a.n_tf + 4) * sizeof(float4), s>>>(a, view);
+cudaError_t launch_forward_train(const TrainArgs& a, int view, int width, int height, int max_grid, cudaStream_t s) {
+  const int slots = ring_slots(width, height, 8, 4);
+  int grid = (slots + 3) / 4;
+  if (grid > max_grid) grid = max_grid;
+  if (grid < 1) grid = 1;
+  forward_train_kernel<<<grid, 128, (size_t)(a.n_tf + 4) * sizeof(float4), s>>>(a, view);
   return cudaGetLastError();
+}
+
+int forward_train_blocks_per_sm(int n_tf) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, forward_train_kernel, 128,
+                                                    (size_t)(n_tf + 4) * sizeof(float4)) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
 }
 
 cudaError_t launch_backward(const TrainArgs& a, int view, int grid, cudaStream_t s) {
@@ -296,6 +428,15 @@ cudaError_t launch_backward(const TrainArgs& a, int view, int grid, cudaStream_t
     if (e != cudaSuccess) return e;
   }
   backward_kernel<<<grid, 128, smem, s>>>(a, view);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fold_quads(const float4* quads, float* out, const int dims[3], cudaStream_t s) {
+  const size_t total = (size_t)dims[0] * dims[1] * dims[2];
+  size_t grid = (total + 255) / 256;
+  if (grid > 152 * 32) grid = 152 * 32;
+  if (grid < 1) grid = 1;
+  fold_quads_kernel<<<(unsigned)grid, 256, 0, s>>>(quads, out, dims[0], total);
   return cudaGetLastError();
 }
 

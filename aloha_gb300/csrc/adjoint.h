@@ -35,18 +35,22 @@ struct TrainArgs {
   float4* out_rgba;           // [npx] caller's image (forward) or null
   uint2* work;                // [work_cap] (pixel, segment)
   unsigned work_cap;
-  unsigned* work_count;
+  unsigned* work_count;        // [0] segments appended, [1] chunk counter of the forward
   int* overflow;              // set when a pixel needs more checkpoints than ckpt_cap
   const float4* dl_drgba;     // [npx] backward input
   float* dtf;                 // [n_tf*4] accumulated
-  float* dgrid;               // density gradient, accumulated
+  float4* dgrid4;             // density gradient in x-quads: element (x,y,z) holds the
+                              // contributions to voxels x, x+1, x+2 (w unused)
   const int4* brick_grid_origin;  // per brick: voxelRange.lower - grid_lo
   int grid_dims[3];
   unsigned long long* counter;
 };
 
-cudaError_t launch_forward_train(const TrainArgs& a, int view, int width, int height, cudaStream_t s);
+cudaError_t launch_forward_train(const TrainArgs& a, int view, int width, int height, int max_grid, cudaStream_t s);
+int forward_train_blocks_per_sm(int n_tf);
 cudaError_t launch_backward(const TrainArgs& a, int view, int grid, cudaStream_t s);
+// out[v] += quads[v].x + quads[v-1].y + quads[v-2].z along x, for a grid of dims.
+cudaError_t launch_fold_quads(const float4* quads, float* out, const int dims[3], cudaStream_t s);
 int backward_blocks_per_sm(int n_tf);
 
 }  // namespace aloha

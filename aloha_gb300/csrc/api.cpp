@@ -95,7 +95,7 @@ struct aloha_ctx {
   std::vector<Box> boxes;
   std::vector<DevBrick> dev_bricks;
   std::vector<char> brick_present;
-  std::vector<size_t> brick_offset;  // float offset of each padded brick in `voxels`
+  std::vector<size_t> brick_offset;  // quad offset of each padded brick in `voxels`
   DeviceBuffer voxels, bricks_dev, staging_in;
   float bounds_lo[3] = {0, 0, 0}, bounds_hi[3] = {0, 0, 0};
   // transfer function
@@ -117,7 +117,11 @@ struct aloha_ctx {
   int sched_stride = 0;  // ints per view slot
   // params, scratch
   aloha_render_params params;
-  DeviceBuffer counter, flag, staging_out;
+  DeviceBuffer counter, flag, staging_out, work, grad4;
+  // persistent render of one view: chunk shape and grid (occupancy depends on
+  // the transfer-function size through shared memory)
+  int chunk_w = 0, chunk_h = 0;  // 0 = automatic
+  int grid_n_tf = -1, grid_blocks = 0, grid_cw = 0, grid_ch = 0;
   uint64_t last_samples = 0;
   bool samples_valid = false;
 
@@ -239,6 +243,37 @@ int prepare_accum(aloha_ctx* c, int view, cudaStream_t s, float4** out) {
     v.accum_elems = elems;
   }
   *out = v.accum;
+  return ALOHA_OK;
+}
+
+// One persistent render launch of a single view (resets the work counter).
+int launch_single(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
+  const ViewState& v = c->views[view];
+  // automatic chunk: 8x8 for large frames, single 8x4 sub-tiles when a frame
+  // has too few chunks to give every resident warp several
+  int cw = c->chunk_w, ch = c->chunk_h;
+  if (cw == 0) {
+    cw = 8;
+    ch = (long long)v.width * v.height >= 512ll * 512ll ? 8 : 4;
+  }
+  if (c->grid_n_tf != c->n_tf || c->grid_cw != cw || c->grid_ch != ch) {
+    const int per_sm = render_blocks_per_sm(cw, ch, c->n_tf);
+    if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "render occupancy query failed");
+    c->grid_blocks = per_sm * c->num_sms;
+    c->grid_n_tf = c->n_tf;
+    c->grid_cw = cw;
+    c->grid_ch = ch;
+  }
+  BatchArgs b{};
+  b.f = f;
+  b.n_items = 1;
+  b.single_view = view;
+  b.total_tiles = ring_slots(v.width, v.height, cw, ch);
+  b.work_counter = static_cast<unsigned int*>(c->work.ptr);
+  const int warps_per_block = kRenderThreads / 32;
+  const int grid = std::max(1, std::min(c->grid_blocks, (b.total_tiles + warps_per_block - 1) / warps_per_block));
+  CUDA_TRY(c, cudaMemsetAsync(c->work.ptr, 0, sizeof(unsigned int), s));
+  CUDA_TRY(c, launch_render_warps(b, cw, ch, grid, s));
   return ALOHA_OK;
 }
 
@@ -392,7 +427,8 @@ int aloha_create(int device, aloha_ctx** out) {
   c->num_sms = prop.multiProcessorCount;
   aloha_default_render_params(&c->params);
   if (c->views_dev.ensure(sizeof(DevView) * kMaxViews) != cudaSuccess ||
-      c->counter.ensure(sizeof(unsigned long long)) != cudaSuccess || c->flag.ensure(sizeof(int)) != cudaSuccess) {
+      c->counter.ensure(sizeof(unsigned long long)) != cudaSuccess || c->flag.ensure(sizeof(int)) != cudaSuccess ||
+      c->work.ensure(sizeof(unsigned int)) != cudaSuccess) {
     delete c;
     return ALOHA_ERR_OUT_OF_MEMORY;
   }
@@ -409,7 +445,8 @@ int aloha_destroy(aloha_ctx* c) {
     v.train.release();
   }
   for (DeviceBuffer* b : {&c->voxels, &c->bricks_dev, &c->staging_in, &c->tf, &c->views_dev, &c->sched_dev,
-                          &c->counter, &c->flag, &c->staging_out, &c->mc_ranges, &c->mc_empty, &c->tf_prefix})
+                          &c->counter, &c->flag, &c->staging_out, &c->mc_ranges, &c->mc_empty, &c->tf_prefix,
+                          &c->work, &c->grad4})
     b->release();
   delete c;
   return ALOHA_OK;
@@ -440,7 +477,7 @@ static int upload_brick(aloha_ctx* c, int b, const float* src) {
     dsrc = static_cast<const float*>(c->staging_in.ptr);
   }
   const DevBrick& db = c->dev_bricks[b];
-  float* alloc = static_cast<float*>(c->voxels.ptr) + c->brick_offset[b];
+  float4* alloc = static_cast<float4*>(c->voxels.ptr) + c->brick_offset[b];
   CUDA_TRY(c, cudaMemset(c->flag.ptr, 0, sizeof(int)));
   CUDA_TRY(c, launch_pad_brick(dsrc, nx, ny, nz, alloc, db.sy, db.sz / db.sy, nz + 2 * kApron,
                                static_cast<int*>(c->flag.ptr), 0));
@@ -472,13 +509,13 @@ int aloha_set_bricks(aloha_ctx* c, const aloha_brick_desc* descs, const float* c
       if (!(std::isfinite(d.space_lo[a]) && std::isfinite(d.space_hi[a]) && d.space_lo[a] < d.space_hi[a]))
         return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "brick %d: empty or non-finite space range", b);
     }
-    // rows padded to a multiple of 8 floats (32-byte aligned rows)
-    const int px = ((nsz[0] + 2 * kApron) + 7) & ~7, py = nsz[1] + 2 * kApron, pz = nsz[2] + 2 * kApron;
+    // rows padded to an even number of quads (32-byte aligned rows)
+    const int px = ((nsz[0] + 2 * kApron) + 1) & ~1, py = nsz[1] + 2 * kApron, pz = nsz[2] + 2 * kApron;
     const size_t elems = (size_t)px * py * pz;
     if (elems >= (size_t)1 << 31)
       return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "brick %d too large for 32-bit voxel offsets; split it", b);
     offs[b] = total;
-    total += (elems + 63) & ~(size_t)63;  // 256-byte aligned bricks
+    total += (elems + 15) & ~(size_t)15;  // 256-byte aligned bricks (in quads)
     db[b].sy = px;
     db[b].sz = px * py;
     for (int a = 0; a < 3; ++a) {
@@ -490,12 +527,12 @@ int aloha_set_bricks(aloha_ctx* c, const aloha_brick_desc* descs, const float* c
   }
   size_t free_b = 0, total_b = 0;
   CUDA_TRY(c, cudaMemGetInfo(&free_b, &total_b));
-  if (total * sizeof(float) > free_b + c->voxels.bytes)
-    return c->fail(ALOHA_ERR_OUT_OF_MEMORY, "bricks need %zu bytes, %zu free", total * sizeof(float), free_b);
+  if (total * sizeof(float4) > free_b + c->voxels.bytes)
+    return c->fail(ALOHA_ERR_OUT_OF_MEMORY, "bricks need %zu bytes, %zu free", total * sizeof(float4), free_b);
   CUDA_TRY(c, cudaDeviceSynchronize());
-  CUDA_TRY(c, c->voxels.ensure(total * sizeof(float)));
+  CUDA_TRY(c, c->voxels.ensure(total * sizeof(float4)));
   for (int b = 0; b < n; ++b)
-    db[b].base = static_cast<const float*>(c->voxels.ptr) + offs[b] + (size_t)kApron * db[b].sz +
+    db[b].base = static_cast<const float4*>(c->voxels.ptr) + offs[b] + (size_t)kApron * db[b].sz +
                  (size_t)kApron * db[b].sy + kApron;
   std::vector<size_t> mc_off(n);
   size_t mc_total = 0;
@@ -654,6 +691,16 @@ int aloha_get_composite_order(aloha_ctx* c, int view, int* rank_order, int max_r
   return ALOHA_OK;
 }
 
+int aloha_set_render_tile(aloha_ctx* c, int tile_w, int tile_h) {
+  if (!c) return ALOHA_ERR_NULL_POINTER;
+  if (!(tile_w == 0 && tile_h == 0) && !known_chunk(tile_w, tile_h))
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "tile %dx%d not one of 0x0 (auto), 8x4, 8x8, 16x8, 32x4", tile_w,
+                   tile_h);
+  c->chunk_w = tile_w;
+  c->chunk_h = tile_h;
+  return ALOHA_OK;
+}
+
 int aloha_render(aloha_ctx* c, int view, uint32_t* fb, void* stream) {
   if (!c || !fb) return ALOHA_ERR_NULL_POINTER;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -673,7 +720,8 @@ int aloha_render(aloha_ctx* c, int view, uint32_t* fb, void* stream) {
     a.fb = fb;
   }
   CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
-  CUDA_TRY(c, launch_render(a, view, v.width, v.height, s));
+  rc = launch_single(c, a, view, s);
+  if (rc) return rc;
   c->samples_valid = true;
   if (host) return finish_host_output(c, fb, a.fb, npx * sizeof(uint32_t), s);
   return ALOHA_OK;
@@ -700,7 +748,8 @@ int aloha_render_partials(aloha_ctx* c, int view, float* rank_images, float* ran
   a.rank_depth = rank_depth ? (host_depth ? reinterpret_cast<float*>(stage + img_bytes) : rank_depth) : nullptr;
   a.fb = nullptr;
   CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
-  CUDA_TRY(c, launch_render(a, view, v.width, v.height, s));
+  rc = launch_single(c, a, view, s);
+  if (rc) return rc;
   c->samples_valid = true;
   if (host_img) CUDA_TRY(c, cudaMemcpyAsync(rank_images, a.rank_images, img_bytes, cudaMemcpyDeviceToHost, s));
   if (host_depth) CUDA_TRY(c, cudaMemcpyAsync(rank_depth, a.rank_depth, depth_bytes, cudaMemcpyDeviceToHost, s));
@@ -881,7 +930,7 @@ int aloha_forward(aloha_ctx* c, int view, float* rgba, int checkpoint_every, voi
     CUDA_TRY(c, cudaMalloc(&t.ckpt, npx * cap * sizeof(Checkpoint)));
     CUDA_TRY(c, cudaMalloc(&t.work, npx * cap * sizeof(uint2)));
     CUDA_TRY(c, cudaMalloc(&t.final_rgba, npx * sizeof(float4)));
-    CUDA_TRY(c, cudaMalloc(&t.work_count, sizeof(unsigned)));
+    CUDA_TRY(c, cudaMalloc(&t.work_count, 2 * sizeof(unsigned)));
     CUDA_TRY(c, cudaMalloc(&t.overflow, sizeof(int)));
     t.npx = npx;
     t.cap = cap;
@@ -891,10 +940,12 @@ int aloha_forward(aloha_ctx* c, int view, float* rgba, int checkpoint_every, voi
   TrainArgs a = train_args(c, t);
   const bool host = !is_device_pointer(rgba);
   a.out_rgba = host ? nullptr : reinterpret_cast<float4*>(rgba);
-  CUDA_TRY(c, cudaMemsetAsync(t.work_count, 0, sizeof(unsigned), s));
+  CUDA_TRY(c, cudaMemsetAsync(t.work_count, 0, 2 * sizeof(unsigned), s));
   CUDA_TRY(c, cudaMemsetAsync(t.overflow, 0, sizeof(int), s));
   CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
-  CUDA_TRY(c, launch_forward_train(a, view, v.width, v.height, s));
+  const int per_sm = forward_train_blocks_per_sm(c->n_tf);
+  if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "forward occupancy query failed");
+  CUDA_TRY(c, launch_forward_train(a, view, v.width, v.height, per_sm * c->num_sms, s));
   c->samples_valid = true;
   t.valid = true;
   if (host) return finish_host_output(c, rgba, t.final_rgba, npx * sizeof(float4), s);
@@ -940,20 +991,25 @@ int aloha_backward(aloha_ctx* c, int view, const float* dl_drgba, float* dl_dtf,
   TrainArgs a = train_args(c, t);
   a.dl_drgba = h_dl ? reinterpret_cast<const float4*>(st) : reinterpret_cast<const float4*>(dl_drgba);
   a.dtf = h_tf ? reinterpret_cast<float*>(st + off_tf) : dl_dtf;
-  a.dgrid = h_grid ? reinterpret_cast<float*>(st + off_grid) : dl_ddensity;
+  float* grid_out = h_grid ? reinterpret_cast<float*>(st + off_grid) : dl_ddensity;
   a.brick_grid_origin = reinterpret_cast<const int4*>(st + off_org);
   for (int k = 0; k < 3; ++k) a.grid_dims[k] = grid_dims[k];
+  // the kernel accumulates into x-quads (vector atomics), folded into the grid afterwards
+  CUDA_TRY(c, c->grad4.ensure(grid_elems * sizeof(float4)));
+  a.dgrid4 = static_cast<float4*>(c->grad4.ptr);
+  CUDA_TRY(c, cudaMemsetAsync(a.dgrid4, 0, grid_elems * sizeof(float4), s));
   if (h_dl) CUDA_TRY(c, cudaMemcpyAsync(st, dl_drgba, npx * sizeof(float4), cudaMemcpyHostToDevice, s));
   if (h_tf) CUDA_TRY(c, cudaMemcpyAsync(a.dtf, dl_dtf, tf_bytes, cudaMemcpyHostToDevice, s));
-  if (h_grid) CUDA_TRY(c, cudaMemcpyAsync(a.dgrid, dl_ddensity, g_bytes, cudaMemcpyHostToDevice, s));
+  if (h_grid) CUDA_TRY(c, cudaMemcpyAsync(grid_out, dl_ddensity, g_bytes, cudaMemcpyHostToDevice, s));
   CUDA_TRY(c, cudaMemcpyAsync(st + off_org, origin.data(), origin.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
   const int per_sm = backward_blocks_per_sm(c->n_tf);
   if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "backward occupancy query failed");
   CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
   CUDA_TRY(c, launch_backward(a, view, c->num_sms * per_sm, s));
+  CUDA_TRY(c, launch_fold_quads(a.dgrid4, grid_out, grid_dims, s));
   c->samples_valid = true;
   if (h_tf) CUDA_TRY(c, cudaMemcpyAsync(dl_dtf, a.dtf, tf_bytes, cudaMemcpyDeviceToHost, s));
-  if (h_grid) CUDA_TRY(c, cudaMemcpyAsync(dl_ddensity, a.dgrid, g_bytes, cudaMemcpyDeviceToHost, s));
+  if (h_grid) CUDA_TRY(c, cudaMemcpyAsync(dl_ddensity, grid_out, g_bytes, cudaMemcpyDeviceToHost, s));
   if (h_dl || h_tf || h_grid) CUDA_TRY(c, cudaStreamSynchronize(s));
   return ALOHA_OK;
 }

@@ -43,13 +43,13 @@ int configure(aloha_batch* b) {
   for (size_t i = 0; i < b->views.size(); ++i) {
     int w = 0, h = 0;
     ctx_view_size(c, b->views[i], &w, &h);
-    const int tiles = ((w + b->tile_w - 1) / b->tile_w) * ((h + b->tile_h - 1) / b->tile_h);
+    const int tiles = ring_slots(w, h, b->tile_w, b->tile_h);
     prefix[i + 1] = prefix[i] + tiles;
   }
   b->total_tiles = prefix.back();
   if (cudaMemcpy(b->d_prefix, prefix.data(), sizeof(int) * prefix.size(), cudaMemcpyHostToDevice) != cudaSuccess)
     return ctx_fail(c, ALOHA_ERR_CUDA, "batch: uploading tile prefix failed");
-  int per_sm = batch_blocks_per_sm(b->tile_w, b->tile_h, ctx_n_tf(c));
+  int per_sm = render_blocks_per_sm(b->tile_w, b->tile_h, ctx_n_tf(c));
   if (per_sm <= 0) return ctx_fail(c, ALOHA_ERR_CUDA, "batch: occupancy query failed");
   if (b->ctas_per_sm > 0 && b->ctas_per_sm < per_sm) per_sm = b->ctas_per_sm;
   b->grid = ctx_num_sms(c) * per_sm;
@@ -70,7 +70,7 @@ int enqueue(aloha_batch* b, cudaStream_t s) {
   if (cudaMemsetAsync(b->d_work, 0, sizeof(unsigned int), s) != cudaSuccess ||
       cudaMemsetAsync(a.f.counter, 0, sizeof(unsigned long long), s) != cudaSuccess)
     return ctx_fail(c, ALOHA_ERR_CUDA, "batch: memset failed");
-  cudaError_t e = launch_render_batch(a, b->tile_w, b->tile_h, b->grid, s);
+  cudaError_t e = launch_render_warps(a, b->tile_w, b->tile_h, b->grid, s);
   if (e != cudaSuccess) return ctx_fail(c, ALOHA_ERR_CUDA, "batch launch: %s", cudaGetErrorString(e));
   ctx_mark_samples(c);
   return ALOHA_OK;
@@ -129,9 +129,9 @@ int aloha_batch_create(aloha_ctx* c, const int* views, int n_items, uint32_t* co
 
 int aloha_batch_set_config(aloha_batch* b, int tile_w, int tile_h, int ctas_per_sm) {
   if (!b) return ALOHA_ERR_NULL_POINTER;
-  const bool known = (tile_w == 8 && tile_h == 8) || (tile_w == 16 && tile_h == 8) || (tile_w == 32 && tile_h == 4);
+  const bool known = known_chunk(tile_w, tile_h);
   if (!known || ctas_per_sm < 0)
-    return ctx_fail(b->ctx, ALOHA_ERR_INVALID_ARGUMENT, "tile %dx%d not one of 8x8, 16x8, 32x4", tile_w, tile_h);
+    return ctx_fail(b->ctx, ALOHA_ERR_INVALID_ARGUMENT, "tile %dx%d not one of 8x4, 8x8, 16x8, 32x4", tile_w, tile_h);
   b->tile_w = tile_w;
   b->tile_h = tile_h;
   b->ctas_per_sm = ctas_per_sm;
@@ -191,7 +191,7 @@ int aloha_batch_autotune(aloha_batch* b, void* stream, int reps, int* tile_w, in
   if (!b || !tile_w || !tile_h || !ms) return ALOHA_ERR_NULL_POINTER;
   if (reps < 1) reps = 1;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  static const int shapes[3][2] = {{8, 8}, {16, 8}, {32, 4}};
+  static const int shapes[4][2] = {{8, 4}, {8, 8}, {16, 8}, {32, 4}};
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     return ctx_fail(b->ctx, ALOHA_ERR_CUDA, "cudaEventCreate failed");

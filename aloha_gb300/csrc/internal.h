@@ -11,6 +11,11 @@ namespace aloha {
 // Padded brick storage: every brick is stored with an apron of kApron voxels
 // on each side, filled with the clamped edge values (cudaAddressModeClamp of
 // waikikiRenderer.cpp:753-755), so the march loop needs no per-tap clamps.
+// Each stored element is an x-quad: the float4 (V(x), V(x+1), V(x+2), V(x+3))
+// (indices clamped), so one 16-byte load fetches the three x columns a
+// stencil row needs.  The march is bound by L1 wavefronts (one per distinct
+// 128-byte line a warp load touches); quads cut the loads per sample from 20
+// to 8 at four times the HBM footprint.
 constexpr int kApron = 2;
 constexpr int kMaxViews = 4096;
 constexpr int kMaxTF = 2048;  // (n + 4) float4 entries stay under 48 KB of shared memory
@@ -22,9 +27,9 @@ constexpr int kMacro = 1 << kMacroShift;
 
 // One brick as the kernels see it (72 bytes).
 struct DevBrick {
-  const float* base;     // voxel (0,0,0) of the voxel range inside the padded array
+  const float4* base;    // x-quad of voxel (0,0,0) of the voxel range inside the padded array
   const uint8_t* empty;  // [mz][my][mx] 1 = every sample there has alpha 0 (null: no skipping)
-  int sy, sz;            // padded row and slice pitch, in floats
+  int sy, sz;            // padded row and slice pitch, in quads
   int n[3];              // voxel range size
   float lo[3];           // voxelRange.lower (voxel-unit origin of the brick)
   float space_lo[3], space_hi[3];
@@ -64,26 +69,47 @@ struct FrameArgs {
   unsigned long long* counter;  // total samples (atomic) or null
 };
 
-// Batched launch: a list of (view, output) pairs processed by one persistent
-// kernel, ray tiles handed out through an atomic work counter.
+// One persistent render launch over a list of (view, output) items: warps
+// pull pixel chunks from an atomic work counter.  A single view leaves
+// view_ids, fbs and tile_prefix null and uses single_view and f.fb.
 struct BatchArgs {
   FrameArgs f;
   const int* view_ids;       // [n_items] view of each batch item
   uint32_t* const* fbs;      // [n_items] output frame buffers (device)
-  const int* tile_prefix;    // [n_items+1] prefix sum of ray tiles per item
+  const int* tile_prefix;    // [n_items+1] prefix sum of chunks per item
   int n_items;
-  int total_tiles;
+  int single_view;
+  int total_tiles;           // chunks in the launch
   unsigned int* work_counter;
 };
 
-cudaError_t launch_render(const FrameArgs& a, int view, int width, int height, cudaStream_t s);
+// Chunk shapes (pixels a warp takes per work-counter grab, rendered as 8x4
+// sub-tiles): 8x4, 8x8, 16x8 or 32x4.
+inline bool known_chunk(int w, int h) {
+  return (w == 8 && h == 4) || (w == 8 && h == 8) || (w == 16 && h == 8) || (w == 32 && h == 4);
+}
+// Chunks are handed out centre-out, in square rings around the image centre
+// (the longest rays usually cross the middle, so they start first and the
+// frame's tail is short).  Work slots cover the smallest odd square of rings
+// that contains the chunk grid; slots outside the grid are skipped.
+__host__ __device__ inline int ring_radius(int cxn, int cyn) {
+  const int cx = (cxn - 1) / 2, cy = (cyn - 1) / 2;
+  int r = cx > cxn - 1 - cx ? cx : cxn - 1 - cx;
+  const int ry = cy > cyn - 1 - cy ? cy : cyn - 1 - cy;
+  return r > ry ? r : ry;
+}
+__host__ __device__ inline int ring_slots(int width, int height, int cw, int ch) {
+  const int r = ring_radius((width + cw - 1) / cw, (height + ch - 1) / ch);
+  return (2 * r + 1) * (2 * r + 1);
+}
+constexpr int kRenderThreads = 128;
 cudaError_t launch_composite_f32(const float4* imgs, const int* order, int n_ranks, int npx, int mode, uint32_t* fb,
                                  cudaStream_t s);
 cudaError_t launch_composite_u8(const uint32_t* imgs, const int* order, int n_ranks, int npx, uint32_t* fb,
                                 cudaStream_t s);
-cudaError_t launch_pad_brick(const float* src, int nx, int ny, int nz, float* dst_alloc, int px, int py, int pz,
+cudaError_t launch_pad_brick(const float* src, int nx, int ny, int nz, float4* dst_alloc, int px, int py, int pz,
                              int* nonfinite_flag, cudaStream_t s);
-cudaError_t launch_render_batch(const BatchArgs& a, int tile_w, int tile_h, int grid, cudaStream_t s);
+cudaError_t launch_render_warps(const BatchArgs& a, int chunk_w, int chunk_h, int grid, cudaStream_t s);
 cudaError_t launch_macrocell_range(const DevBrick& b, float2* out, cudaStream_t s);
 cudaError_t launch_macrocell_empty(const float2* ranges, int count, const int* prefix, int n, uint8_t* empty,
                                    cudaStream_t s);
@@ -91,7 +117,7 @@ inline int macrocells(const DevBrick& b) {
   return ((b.n[0] + kMacro - 1) >> kMacroShift) * ((b.n[1] + kMacro - 1) >> kMacroShift) *
          ((b.n[2] + kMacro - 1) >> kMacroShift);
 }
-// CTAs of the batched kernel that fit on one SM for a tile shape (0 if the shape is unknown).
-int batch_blocks_per_sm(int tile_w, int tile_h, int n_tf);
+// CTAs of the render kernel that fit on one SM for a chunk shape (0 if the shape is unknown).
+int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf);
 
 }  // namespace aloha

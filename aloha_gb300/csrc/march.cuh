@@ -10,8 +10,9 @@
 // tap is the trilinear interpolation at u, the six gradient taps sit at
 // u +- 1/2 (the reference's tc +- 0.5/N, deviceCode.cpp:278-284).  u - 1/2 and
 // u + 1/2 differ by exactly 1, so all seven taps read one 20-voxel cross
-// around the cell and share their fractional weights: 20 loads per sample
-// instead of 56.
+// around the cell and share their fractional weights.  With the x-quad brick
+// layout the cross is 4 16-byte and 4 8-byte loads per sample (56 texel
+// fetches in the reference).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -95,8 +96,8 @@ struct StencilOut {
   float value, gx, gy, gz;
 };
 
-__device__ __forceinline__ StencilOut stencil(const float* __restrict__ base, int sy, int sz, int nx, int ny, int nz,
-                                              float ux, float uy, float uz) {
+__device__ __forceinline__ StencilOut stencil(const float4* __restrict__ base, int sy, int sz, int nx, int ny,
+                                              int nz, float ux, float uy, float uz) {
   const float mx = ux - 0.5f, my = uy - 0.5f, mz = uz - 0.5f;
   const float fmx = floorf(mx), fmy = floorf(my), fmz = floorf(mz);
   const float fcx = floorf(ux), fcy = floorf(uy), fcz = floorf(uz);
@@ -113,19 +114,24 @@ __device__ __forceinline__ StencilOut stencil(const float* __restrict__ base, in
   const int cy = min(max((int)fcy, -kApron), ny);
   const int cz = min(max((int)fcz, -kApron), nz);
 
-  // X region: x in {ix, ix+1, ix+2}, y in {cy, cy+1}, z in {cz, cz+1}.
-  const float* p0 = base + (cz * sz + cy * sy + ix);
-  const float a000 = __ldg(p0), a100 = __ldg(p0 + 1), a200 = __ldg(p0 + 2);
-  const float a010 = __ldg(p0 + sy), a110 = __ldg(p0 + sy + 1), a210 = __ldg(p0 + sy + 2);
-  const float a001 = __ldg(p0 + sz), a101 = __ldg(p0 + sz + 1), a201 = __ldg(p0 + sz + 2);
-  const float a011 = __ldg(p0 + sz + sy), a111 = __ldg(p0 + sz + sy + 1), a211 = __ldg(p0 + sz + sy + 2);
-  // Extra y row (iy or iy+2) and extra z slice (iz or iz+2) at x in {cx, cx+1}.
+  // X region: x in {ix, ix+1, ix+2}, y in {cy, cy+1}, z in {cz, cz+1}: one
+  // quad per (y, z) row.
+  const float4* p0 = base + (cz * sz + cy * sy + ix);
+  const float4 r00 = __ldg(p0), r10 = __ldg(p0 + sy), r01 = __ldg(p0 + sz), r11 = __ldg(p0 + sz + sy);
+  const float a000 = r00.x, a100 = r00.y, a200 = r00.z;
+  const float a010 = r10.x, a110 = r10.y, a210 = r10.z;
+  const float a001 = r01.x, a101 = r01.y, a201 = r01.z;
+  const float a011 = r11.x, a111 = r11.y, a211 = r11.z;
+  // Extra y row (iy or iy+2) and extra z slice (iz or iz+2) at x in {cx, cx+1}:
+  // the first half of a quad.
   const int ye = hy ? iy : iy + 2;
   const int ze = hz ? iz : iz + 2;
-  const float* p1 = base + (cz * sz + ye * sy + cx);
-  const float b00 = __ldg(p1), b10 = __ldg(p1 + 1), b01 = __ldg(p1 + sz), b11 = __ldg(p1 + sz + 1);
-  const float* p2 = base + (ze * sz + cy * sy + cx);
-  const float c00 = __ldg(p2), c10 = __ldg(p2 + 1), c01 = __ldg(p2 + sy), c11 = __ldg(p2 + sy + 1);
+  const float4* p1 = base + (cz * sz + ye * sy + cx);
+  const float2 e0 = __ldg(reinterpret_cast<const float2*>(p1)), e1 = __ldg(reinterpret_cast<const float2*>(p1 + sz));
+  const float b00 = e0.x, b10 = e0.y, b01 = e1.x, b11 = e1.y;
+  const float4* p2 = base + (ze * sz + cy * sy + cx);
+  const float2 f0 = __ldg(reinterpret_cast<const float2*>(p2)), f1 = __ldg(reinterpret_cast<const float2*>(p2 + sy));
+  const float c00 = f0.x, c10 = f0.y, c01 = f1.x, c11 = f1.y;
 
   // x taps: columns X_k = bilinear (y by gy, then z by gz) at x = ix + k.
   const float X0 = lerpf(lerpf(a000, a010, gy), lerpf(a001, a011, gy), gz);
@@ -207,38 +213,50 @@ __device__ __forceinline__ uint32_t march_cap(float t0, float t1, float dt) {
 __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
                                                 const Ray& r, float t0, float t1, float ils, float dt, float et,
                                                 float4& color) {
-  const float* __restrict__ base = b.base;
+  const float4* __restrict__ base = b.base;
   const int sy = b.sy, sz = b.sz, nx = b.n[0], ny = b.n[1], nz = b.n[2];
   const float lox = b.lo[0], loy = b.lo[1], loz = b.lo[2];
   const float nf = (float)n_tf;
   const uint32_t cap = march_cap(t0, t1, dt);
   const uint8_t* __restrict__ empty = b.empty;
   const int mnx = (nx + kMacro - 1) >> kMacroShift, mny = (ny + kMacro - 1) >> kMacroShift;
+  // Brick-local ray origin, inverse direction and the rounding margin (voxel
+  // units) that makes the macrocell exit bound below conservative: u = o + t d
+  // - lo is computed with a few ulps of the largest magnitude involved.
+  const float offx = r.o[0] - lox, offy = r.o[1] - loy, offz = r.o[2] - loz;
+  const float idx_ = 1.0f / r.d[0], idy = 1.0f / r.d[1], idz = 1.0f / r.d[2];
+  const float mag = fmaxf(fmaxf(fabsf(r.o[0]) + fabsf(lox), fabsf(r.o[1]) + fabsf(loy)),
+                          fabsf(r.o[2]) + fabsf(loz)) + fabsf(t1);
+  const float eps = 2e-6f * mag + 1e-4f;
   uint32_t n = 0;
   float t = first_sample_t(t0, dt, ils);
   while (t < t1 && color.w < et && n < cap) {
-    float ux = fmaf(t, r.d[0], r.o[0]) - lox;
-    float uy = fmaf(t, r.d[1], r.o[1]) - loy;
-    float uz = fmaf(t, r.d[2], r.o[2]) - loz;
+    const float ux = fmaf(t, r.d[0], r.o[0]) - lox;
+    const float uy = fmaf(t, r.d[1], r.o[1]) - loy;
+    const float uz = fmaf(t, r.d[2], r.o[2]) - loz;
     if (empty) {
-      // Run through empty space: a sample in an empty macrocell has alpha
-      // exactly 0 and leaves the colour unchanged, so only t and the sample
-      // count advance (the same t += dt sequence as a full sample).
-      bool done = false;
-      while (__ldg(empty + ((min(max((int)floorf(uz), 0), nz - 1) >> kMacroShift) * mny +
-                            (min(max((int)floorf(uy), 0), ny - 1) >> kMacroShift)) * mnx +
-                   (min(max((int)floorf(ux), 0), nx - 1) >> kMacroShift))) {
+      const int mx = min(max((int)floorf(ux), 0), nx - 1) >> kMacroShift;
+      const int my = min(max((int)floorf(uy), 0), ny - 1) >> kMacroShift;
+      const int mz = min(max((int)floorf(uz), 0), nz - 1) >> kMacroShift;
+      if (__ldg(empty + (mz * mny + my) * mnx + mx)) {
+        // Empty macrocell: a sample there has alpha exactly 0 and leaves the
+        // colour unchanged, so only t and the sample count advance (the same
+        // t += dt sequence as full samples).  Every sample before tb, the
+        // ray's exit from the macrocell's box shrunk by eps, lies in this
+        // macrocell; the exact test resumes after it.
+        const float bx = (float)(mx << kMacroShift), by = (float)(my << kMacroShift), bz = (float)(mz << kMacroShift);
+        const float ex = ((r.d[0] > 0.f ? bx + (float)kMacro - eps : bx + eps) - offx) * idx_;
+        const float ey = ((r.d[1] > 0.f ? by + (float)kMacro - eps : by + eps) - offy) * idy;
+        const float ez = ((r.d[2] > 0.f ? bz + (float)kMacro - eps : bz + eps) - offz) * idz;
+        const float tb = fminf(fminf(fminf(ex, ey), ez), t1);
         ++n;
         t = t + dt;
-        if (!(t < t1 && n < cap)) {
-          done = true;
-          break;
+        while (t < tb && n < cap) {
+          ++n;
+          t = t + dt;
         }
-        ux = fmaf(t, r.d[0], r.o[0]) - lox;
-        uy = fmaf(t, r.d[1], r.o[1]) - loy;
-        uz = fmaf(t, r.d[2], r.o[2]) - loz;
+        continue;
       }
-      if (done) break;
     }
     ++n;
     const StencilOut s = stencil(base, sy, sz, nx, ny, nz, ux, uy, uz);
@@ -387,6 +405,37 @@ __device__ __forceinline__ uint32_t render_pixel(const FrameArgs& a, const DevVi
   }
   if (a.pixel_samples) a.pixel_samples[pixel] = total;
   return total;
+}
+
+// Work slot k of a view -> chunk (cx, cy) in centre-out square rings; false
+// for slots outside the chunk grid.  Ring r >= 1 holds slots
+// [(2r-1)^2, (2r+1)^2), walked up the right edge, left along the top, down
+// the left edge and right along the bottom.
+__device__ __forceinline__ bool ring_chunk(int k, int cxn, int cyn, int& cx, int& cy) {
+  int x = 0, y = 0;
+  if (k > 0) {
+    int r = (int)((sqrtf((float)k) + 1.0f) * 0.5f);
+    while ((2 * r + 1) * (2 * r + 1) <= k) ++r;
+    while (r > 1 && (2 * r - 1) * (2 * r - 1) > k) --r;
+    const int j = k - (2 * r - 1) * (2 * r - 1);
+    const int side = j / (2 * r), off = j % (2 * r);
+    if (side == 0) {
+      x = r;
+      y = -r + 1 + off;
+    } else if (side == 1) {
+      x = r - 1 - off;
+      y = r;
+    } else if (side == 2) {
+      x = -r;
+      y = r - 1 - off;
+    } else {
+      x = -r + 1 + off;
+      y = -r;
+    }
+  }
+  cx = x + (cxn - 1) / 2;
+  cy = y + (cyn - 1) / 2;
+  return cx >= 0 && cx < cxn && cy >= 0 && cy < cyn;
 }
 
 // Warp-aggregated add of per-thread sample counts into a 64-bit counter.

@@ -8,66 +8,52 @@
 
 namespace aloha {
 
-// Ray tiles: a CTA covers TW x TH pixels; each warp an 8 x 4 block, so the 32
-// rays of a warp start within a few voxels of each other and walk the same
-// cache lines.
-template <int TW, int TH>
-struct TileMap {
-  static constexpr int kThreads = TW * TH;
-  static constexpr int kWarpsX = TW / 8;
-  __device__ __forceinline__ static void pixel(int tid, int& px, int& py) {
-    const int w = tid >> 5, lane = tid & 31;
-    px = (w % kWarpsX) * 8 + (lane & 7);
-    py = (w / kWarpsX) * 4 + (lane >> 3);
-  }
-};
-
-template <int TW, int TH>
-__global__ void __launch_bounds__(TW* TH) render_view_kernel(FrameArgs a, int view) {
+// Persistent render: every warp pulls CW x CH pixel chunks of the launch's
+// items (views) from one atomic counter, centre-out per view, and renders
+// each chunk as 8 x 4-pixel sub-tiles, so the 32 rays of a warp start within
+// a few voxels of each other.  Warps are independent (no barrier after the
+// transfer function is staged): a warp with long rays never holds finished
+// warps of its CTA, and views end without a per-launch tail.  Nothing waits
+// on other warps or CTAs.
+// Six CTAs of 128 threads per SM (80 registers, no spills) keep 24 warps
+// resident to hide the gather latency of the march.
+template <int CW, int CH>
+__global__ void __launch_bounds__(kRenderThreads, 6) render_warps_kernel(BatchArgs b) {
   extern __shared__ float4 tf_s[];
-  load_tf(tf_s, a.tf, a.n_tf);
-  __syncthreads();
-  const DevView v = a.views[view];
-  int px, py;
-  TileMap<TW, TH>::pixel(threadIdx.x, px, py);
-  const int x = blockIdx.x * TW + px, y = blockIdx.y * TH + py;
-  uint32_t n = 0;
-  if (x < v.width && y < v.height) n = render_pixel(a, v, tf_s, x, y, a.fb, (size_t)x + (size_t)v.width * y);
-  count_samples(a.counter, n);
-}
-
-// Persistent batched render: CTAs pull ray tiles of all batch items from one
-// atomic counter until the batch is done (no waiting on other CTAs).
-template <int TW, int TH>
-__global__ void __launch_bounds__(TW* TH) render_batch_kernel(BatchArgs b) {
-  extern __shared__ float4 tf_s[];
-  __shared__ int s_tile;
   load_tf(tf_s, b.f.tf, b.f.n_tf);
-  int px, py;
-  TileMap<TW, TH>::pixel(threadIdx.x, px, py);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
   uint32_t n = 0;
   for (;;) {
-    __syncthreads();
-    if (threadIdx.x == 0) s_tile = (int)atomicAdd(b.work_counter, 1u);
-    __syncthreads();
-    const int tile = s_tile;
-    if (tile >= b.total_tiles) break;
-    // item = last index with tile_prefix[item] <= tile
-    int lo = 0, hi = b.n_items - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (__ldg(b.tile_prefix + mid) <= tile)
-        lo = mid;
-      else
-        hi = mid - 1;
+    int chunk = 0;
+    if (lane == 0) chunk = (int)atomicAdd(b.work_counter, 1u);
+    chunk = __shfl_sync(0xffffffffu, chunk, 0);
+    if (chunk >= b.total_tiles) break;
+    int item = 0, first = 0;
+    if (b.tile_prefix) {
+      // item = last index with tile_prefix[item] <= chunk
+      int lo = 0, hi = b.n_items - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(b.tile_prefix + mid) <= chunk)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      item = lo;
+      first = __ldg(b.tile_prefix + item);
     }
-    const int item = lo;
-    const DevView v = b.f.views[__ldg(b.view_ids + item)];
-    const int tiles_x = (v.width + TW - 1) / TW;
-    const int local = tile - __ldg(b.tile_prefix + item);
-    const int x = (local % tiles_x) * TW + px, y = (local / tiles_x) * TH + py;
-    if (x < v.width && y < v.height)
-      n += render_pixel(b.f, v, tf_s, x, y, b.fbs[item], (size_t)x + (size_t)v.width * y);
+    const DevView v = b.f.views[b.view_ids ? __ldg(b.view_ids + item) : b.single_view];
+    uint32_t* fb = b.fbs ? b.fbs[item] : b.f.fb;
+    int ccx, ccy;
+    if (!ring_chunk(chunk - first, (v.width + CW - 1) / CW, (v.height + CH - 1) / CH, ccx, ccy)) continue;
+    const int x0 = ccx * CW, y0 = ccy * CH;
+#pragma unroll 1
+    for (int sub = 0; sub < (CW / 8) * (CH / 4); ++sub) {
+      const int x = x0 + (sub % (CW / 8)) * 8 + (lane & 7);
+      const int y = y0 + (sub / (CW / 8)) * 4 + (lane >> 3);
+      if (x < v.width && y < v.height) n += render_pixel(b.f, v, tf_s, x, y, fb, (size_t)x + (size_t)v.width * y);
+    }
   }
   count_samples(b.f.counter, n);
 }
@@ -117,28 +103,31 @@ __global__ void composite_u8_kernel(const uint32_t* __restrict__ imgs, const int
   }
 }
 
-// Copies a brick (x fastest) into its padded array, filling the apron with
-// clamped edge values, and flags non-finite voxels.
-__global__ void pad_brick_kernel(const float* __restrict__ src, int nx, int ny, int nz, float* __restrict__ dst,
+// Copies a brick (x fastest) into its padded x-quad array: element (x,y,z)
+// holds V(x..x+3) with every index clamped to the brick (the apron and the
+// quad tails repeat edge values), and flags non-finite voxels.
+__global__ void pad_brick_kernel(const float* __restrict__ src, int nx, int ny, int nz, float4* __restrict__ dst,
                                  int px, int py, int pz, int* nonfinite) {
   const size_t total = (size_t)px * py * pz;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
     const int x = (int)(i % px);
     const int y = (int)((i / px) % py);
     const int z = (int)(i / ((size_t)px * py));
-    const int sx = min(max(x - kApron, 0), nx - 1);
     const int sy = min(max(y - kApron, 0), ny - 1);
     const int sz = min(max(z - kApron, 0), nz - 1);
-    const float v = src[((size_t)sz * ny + sy) * nx + sx];
-    if (!isfinite(v)) atomicOr(nonfinite, 1);
-    dst[i] = v;
+    const float* row = src + ((size_t)sz * ny + sy) * nx;
+    float v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = row[min(max(x - kApron + k, 0), nx - 1)];
+    if (!isfinite(v[0]) || !isfinite(v[1]) || !isfinite(v[2]) || !isfinite(v[3])) atomicOr(nonfinite, 1);
+    dst[i] = make_float4(v[0], v[1], v[2], v[3]);
   }
 }
 
 // Value range each macrocell's samples can read: a sample whose value-tap
 // cell is c (c = clamp(floor(u), 0, n-1)) reads voxels c and c+1 (clamped), so
 // macrocell m covers voxels [m*kMacro, m*kMacro + kMacro] per axis.
-__global__ void macrocell_range_kernel(const float* __restrict__ base, int sy, int sz, int nx, int ny, int nz,
+__global__ void macrocell_range_kernel(const float4* __restrict__ base, int sy, int sz, int nx, int ny, int nz,
                                        int mnx, int mny, int mnz, float2* __restrict__ out) {
   const int total = mnx * mny * mnz;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
@@ -148,9 +137,9 @@ __global__ void macrocell_range_kernel(const float* __restrict__ base, int sy, i
     float lo = __int_as_float(0x7f800000), hi = -lo;
     for (int z = z0; z <= z1; ++z)
       for (int y = y0; y <= y1; ++y) {
-        const float* row = base + (size_t)z * sz + (size_t)y * sy;
+        const float4* row = base + (size_t)z * sz + (size_t)y * sy;
         for (int x = x0; x <= x1; ++x) {
-          const float v = __ldg(row + x);
+          const float v = __ldg(row + x).x;
           lo = fminf(lo, v);
           hi = fmaxf(hi, v);
         }
@@ -196,36 +185,33 @@ cudaError_t launch_macrocell_empty(const float2* ranges, int count, const int* p
   return cudaGetLastError();
 }
 
-cudaError_t launch_render(const FrameArgs& a, int view, int width, int height, cudaStream_t s) {
-  constexpr int TW = 16, TH = 8;
-  dim3 grid((width + TW - 1) / TW, (height + TH - 1) / TH);
-  render_view_kernel<TW, TH><<<grid, TW * TH, tf_smem(a.n_tf), s>>>(a, view);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_render_batch(const BatchArgs& b, int tile_w, int tile_h, int grid, cudaStream_t s) {
+cudaError_t launch_render_warps(const BatchArgs& b, int chunk_w, int chunk_h, int grid, cudaStream_t s) {
   const size_t smem = tf_smem(b.f.n_tf);
-  if (tile_w == 8 && tile_h == 8)
-    render_batch_kernel<8, 8><<<grid, 64, smem, s>>>(b);
-  else if (tile_w == 16 && tile_h == 8)
-    render_batch_kernel<16, 8><<<grid, 128, smem, s>>>(b);
-  else if (tile_w == 32 && tile_h == 4)
-    render_batch_kernel<32, 4><<<grid, 128, smem, s>>>(b);
+  if (chunk_w == 8 && chunk_h == 4)
+    render_warps_kernel<8, 4><<<grid, kRenderThreads, smem, s>>>(b);
+  else if (chunk_w == 8 && chunk_h == 8)
+    render_warps_kernel<8, 8><<<grid, kRenderThreads, smem, s>>>(b);
+  else if (chunk_w == 16 && chunk_h == 8)
+    render_warps_kernel<16, 8><<<grid, kRenderThreads, smem, s>>>(b);
+  else if (chunk_w == 32 && chunk_h == 4)
+    render_warps_kernel<32, 4><<<grid, kRenderThreads, smem, s>>>(b);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 
-int batch_blocks_per_sm(int tile_w, int tile_h, int n_tf) {
+int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf) {
   int n = 0;
   const size_t smem = tf_smem(n_tf);
   cudaError_t e = cudaErrorInvalidValue;
-  if (tile_w == 8 && tile_h == 8)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_batch_kernel<8, 8>, 64, smem);
-  else if (tile_w == 16 && tile_h == 8)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_batch_kernel<16, 8>, 128, smem);
-  else if (tile_w == 32 && tile_h == 4)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_batch_kernel<32, 4>, 128, smem);
+  if (chunk_w == 8 && chunk_h == 4)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_warps_kernel<8, 4>, kRenderThreads, smem);
+  else if (chunk_w == 8 && chunk_h == 8)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_warps_kernel<8, 8>, kRenderThreads, smem);
+  else if (chunk_w == 16 && chunk_h == 8)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_warps_kernel<16, 8>, kRenderThreads, smem);
+  else if (chunk_w == 32 && chunk_h == 4)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_warps_kernel<32, 4>, kRenderThreads, smem);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return 0;
@@ -250,7 +236,7 @@ cudaError_t launch_composite_u8(const uint32_t* imgs, const int* order, int n_ra
   return cudaGetLastError();
 }
 
-cudaError_t launch_pad_brick(const float* src, int nx, int ny, int nz, float* dst, int px, int py, int pz,
+cudaError_t launch_pad_brick(const float* src, int nx, int ny, int nz, float4* dst, int px, int py, int pz,
                              int* nonfinite, cudaStream_t s) {
   const size_t total = (size_t)px * py * pz;
   size_t g = (total + 255) / 256;

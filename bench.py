@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU work of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--only-adjoint", action="store_true",
+                    help="run only the 128^3, 16 x 256^2 forward + adjoint configuration and print its timings")
     ap.add_argument("--profile", action="store_true", help="short run for ncu (no baselines, no clocks)")
     return ap.parse_args()
 
@@ -253,6 +256,7 @@ def main():
     import torch.distributed as dist
 
     from aloha_gb300 import abi
+    from aloha_gb300.replicas import max_over_ranks, shard_views, sum_over_ranks
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -261,6 +265,14 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.only_adjoint:
+        from aloha_gb300 import scenes as S
+        v4 = S.blob_field((128, 128, 128), 16, (4.0, 12.0), seed=4001, device=dev)
+        c4 = S.orbit_cameras((128, 128, 128), 16, 256, 256, seed=4002)
+        res = adjoint_section("128^3 single brick, 16 x 256^2", v4, S.single_brick((128, 128, 128)), c4, 256, 256,
+                              32, torch.cuda.current_stream(), dev)
+        print(json.dumps(res), flush=True)
+        return
 
     def barrier():
         if world > 1:
@@ -275,7 +287,7 @@ def main():
     ctx.set_ranks(8)
     ctx.set_params()
     # replicas only: rank r renders cameras r, r+N, ...
-    mine = list(range(rank, len(cams), world))
+    mine = shard_views(len(cams), rank, world)
     stream = torch.cuda.Stream(device=dev)
     fb = torch.zeros((H, W), dtype=torch.int32, device=dev)
 
@@ -288,6 +300,27 @@ def main():
             ctx.render(0, fb, stream)
             samples_of[ci] = ctx.stats().samples
             bytes_of[ci] = algorithmic_bytes(descs, bricks_hit(descs, cams[ci], W, H), tf.shape[0], W, H)
+
+    # ray-tile sweep of the persistent single-view render (untimed)
+    tile_ms = {}
+    for tw, th in ((8, 8), (16, 8), (32, 4)):
+        ctx.set_render_tile(tw, th)
+        probe = mine[:8]
+        for ci in probe[:2]:
+            ctx.set_camera(0, *cams[ci])
+            ctx.render(0, fb, stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ms = 0.0
+        for ci in probe:
+            ctx.set_camera(0, *cams[ci])
+            e0.record(stream)
+            ctx.render(0, fb, stream)
+            e1.record(stream)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1)
+        tile_ms[f"{tw}x{th}"] = ms / len(probe)
+    best_tile = min(tile_ms, key=tile_ms.get)
+    ctx.set_render_tile(*(int(v) for v in best_tile.split("x")))
 
     steps = [mine[k % len(mine)] for k in range(args.steps)]
     for k in range(args.warmup):
@@ -309,13 +342,8 @@ def main():
     elapsed_ms = t_start.elapsed_time(t_end)
     launch_ms = [e0.elapsed_time(e1) for e0, e1 in ev]
     total_samples = sum(samples_of[ci] for ci in steps)
-    if world > 1:
-        t = torch.tensor([elapsed_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-        s = torch.tensor([total_samples], dtype=torch.float64, device=dev)
-        dist.all_reduce(s)
-        total_samples = int(s.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, dev)
+    total_samples = int(sum_over_ranks(total_samples, dev))
     value = total_samples / (elapsed_ms * 1e-3) / 1e9
 
     # roofline of the fused render kernel: algorithmic bytes / launch duration
@@ -323,7 +351,7 @@ def main():
     mean_launch = float(np.mean(launch_ms))
     peak, peak_kind = measured_peaks()
     achieved = mean_bytes / (mean_launch * 1e-3) / 1e9
-    traffic = profile_traffic("render_view_kernel")
+    traffic = profile_traffic("render_warps_kernel")
 
     result = {"metric": METRIC, "value": value, "unit": "Gsamples/s", "n_gpus": world, "steps": args.steps,
               "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
@@ -337,7 +365,8 @@ def main():
               "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                            "frac": achieved / peak, "peak_kind": peak_kind,
                            "traffic": traffic["bytes_per_launch"] if traffic else None,
-                           "kernel": "render_view_kernel<16,8>",
+                           "kernel": f"render_warps_kernel<{best_tile.replace('x', ',')}>",
+                           "tile_sweep_ms": tile_ms,
                            "algorithmic_bytes_per_launch": mean_bytes, "launch_ms": mean_launch}}
     clocks = clk.summary()
     if clocks:
@@ -356,10 +385,7 @@ def main():
             ctx.render(0, fb_host, stream)
         barrier()
         e2e_s = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([e2e_s], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, dev)
         sched_bytes = 4 * (2 * 8 + 1 + 8)
         result["e2e"] = {"value": total_samples / e2e_s / 1e9, "unit": "Gsamples/s",
                          "ms_per_frame": e2e_s / args.steps * 1e3,
@@ -367,6 +393,18 @@ def main():
 
         if not args.no_batched and rank == 0:
             result["batched"] = batched_section(ctx, cams, mine, W, H, args, stream, dev, samples_of)
+
+        if not args.no_adjoint and rank == 0:
+            from aloha_gb300 import scenes as S
+            # the headline volume and image as one virtual rank
+            adj = [adjoint_section("512^3 @1024^2, 8 bricks as 1 rank", vol, descs, cams[:4], W, H, 32, stream,
+                                   dev)]
+            # the differentiable configuration: 128^3 single brick, 16 views at 256^2, K = 32
+            v4 = S.blob_field((128, 128, 128), 16, (4.0, 12.0), seed=4001, device=dev)
+            c4 = S.orbit_cameras((128, 128, 128), 16, 256, 256, seed=4002)
+            adj.append(adjoint_section("128^3 single brick, 16 x 256^2", v4, S.single_brick((128, 128, 128)), c4,
+                                       256, 256, 32, stream, dev))
+            result["adjoint"] = adj
 
         if not args.no_cpu_baseline and rank == 0:
             vol_np = vol.cpu().numpy()
@@ -381,6 +419,70 @@ def main():
     ctx.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+def adjoint_section(name, vol, descs, cams, W, H, k, stream, dev):
+    """Forward (checkpoints every k samples) and adjoint of an L2 image loss
+    over `cams` views of one virtual rank; times both with CUDA events."""
+    import torch
+
+    from aloha_gb300 import abi
+    from aloha_gb300 import scenes as S
+    from aloha_gb300 import volfile as V
+    ctx = abi.Context(dev.index or 0)
+    vox = [V.brick_voxels(vol, d) for d in descs]
+    ctx.set_bricks(descs, vox)
+    ctx.set_ranks(1)
+    ctx.set_params()
+    n = vol.shape[0]
+    for v, cam in enumerate(cams):
+        ctx.set_camera(v, *cam)
+        ctx.resize(v, W, H)
+    nv = len(cams)
+    target = torch.empty((nv, H, W, 4), dtype=torch.float32, device=dev)
+    ctx.set_transfer_function(S.seeded_tf(77))
+    for v in range(nv):
+        ctx.forward(v, target[v], k, stream)
+    ctx.set_transfer_function(S.ramp_tf())
+    img = torch.empty_like(target)
+    dtf = torch.zeros((256, 4), dtype=torch.float32, device=dev)
+    dden = torch.zeros(tuple(vol.shape), dtype=torch.float32, device=dev)
+
+    def fwd():
+        for v in range(nv):
+            ctx.forward(v, img[v], k, stream)
+
+    def bwd(grad):
+        for v in range(nv):
+            ctx.backward(v, grad[v], dtf, dden, (0, 0, 0), (n, n, n), stream)
+
+    fwd()
+    grad = (2.0 * (img - target)).contiguous()
+    bwd(grad)
+    torch.cuda.synchronize()
+    samples = 0
+    for v in range(nv):
+        ctx.forward(v, img[v], k, stream)
+        samples += ctx.stats().samples
+    reps = 3
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    fwd_ms, bwd_ms = 0.0, 0.0
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        e[0].record(stream)
+        fwd()
+        e[1].record(stream)
+        bwd(grad)
+        e[2].record(stream)
+        torch.cuda.synchronize()
+        fwd_ms += e[0].elapsed_time(e[1]) / reps
+        bwd_ms += e[1].elapsed_time(e[2]) / reps
+    ctx.close()
+    return {"config": name, "views": nv, "image": [W, H], "checkpoint_every": k,
+            "fwd_ms_per_view": fwd_ms / nv, "adjoint_ms_per_view": bwd_ms / nv,
+            "fwd_plus_adjoint_over_fwd": (fwd_ms + bwd_ms) / fwd_ms,
+            "fwd_gsamples_per_s": samples / (fwd_ms * 1e-3) / 1e9,
+            "fwd_plus_adjoint_gsamples_per_s": samples / ((fwd_ms + bwd_ms) * 1e-3) / 1e9}
 
 
 def batched_section(ctx, cams, mine, W, H, args, stream, dev, samples_of):

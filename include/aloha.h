@@ -134,6 +134,12 @@ int aloha_resize(aloha_ctx* ctx, int view, int width, int height);
  * waikikiRenderer.cpp:281-316, or the face-based order). */
 int aloha_get_composite_order(aloha_ctx* ctx, int view, int* rank_order, int max_ranks, int* n_ranks);
 
+/* Pixel chunk a warp of the persistent render takes per grab (rendered as
+ * 8x4-pixel sub-tiles): 8x4, 8x8, 16x8 or 32x4; 0x0 (the default) picks 8x8
+ * for frames of 512^2 pixels or more and 8x4 below.  No reference
+ * counterpart (the raygen launches one thread per pixel). */
+int aloha_set_render_tile(aloha_ctx* ctx, int tile_w, int tile_h);
+
 /* Render one view into an RGBA8 frame buffer of width*height uint32
  * (Renderer::render, waikikiRenderer.cpp:1015-1080): all virtual ranks march
  * their bricks and their images are composited in one fused kernel. */

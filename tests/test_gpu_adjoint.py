@@ -110,10 +110,16 @@ def test_central_differences(gpu_ctx_factory, et):
         ctx.backward(v, weights[v].astype(np.float32), dtf, dden, (0, 0, 0), (n, n, n))
     eps = 1e-3
     errs = []
-    big_tf = np.argwhere(np.abs(dtf) > 0.05 * np.abs(dtf).max())
-    big_den = np.argwhere(np.abs(dden) > 0.05 * np.abs(dden).max())
-    picks = [("tf", tuple(i)) for i in big_tf[rng.choice(len(big_tf), 32, replace=False)]]
-    picks += [("den", tuple(i)) for i in big_den[rng.choice(len(big_den), 32, replace=False)]]
+    def candidates(g, k=128):
+        # the k entries of largest |gradient| (finite differences of tiny
+        # gradients are dominated by fp32 rounding of the loss)
+        flat = np.argsort(-np.abs(g).ravel())[:k]
+        flat = flat[np.abs(g.ravel()[flat]) > 0]
+        return [np.unravel_index(i, g.shape) for i in flat]
+
+    big_tf, big_den = candidates(dtf), candidates(dden)
+    picks = [("tf", tuple(int(v) for v in big_tf[i])) for i in rng.choice(len(big_tf), 32, replace=False)]
+    picks += [("den", tuple(int(v) for v in big_den[i])) for i in rng.choice(len(big_den), 32, replace=False)]
     for kind, idx in picks:
         if kind == "tf":
             f = []
@@ -164,7 +170,7 @@ def test_autograd_function(gpu_ctx_factory):
     with torch.no_grad():
         tf2 = (tf_t - 1e-3 * tf_t.grad / tf_t.grad.abs().max()).clamp(0, 1)
         loss2 = ((render_views(r, tf2, den, [0, 1, 2], (W, W)) - target) ** 2).sum()
-    assert float(loss2) < float(loss)
+    assert float(loss2) < float(loss.detach())
     r.close()
 
 
