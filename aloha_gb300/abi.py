@@ -33,7 +33,7 @@ EXPORTS = [
     "aloha_composite_over", "aloha_composite_over_rgba8", "aloha_get_stats", "aloha_batch_create",
     "aloha_batch_set_config", "aloha_batch_get_config", "aloha_batch_launch", "aloha_batch_launch_graph",
     "aloha_batch_autotune", "aloha_batch_destroy", "aloha_render_batch", "aloha_forward", "aloha_backward",
-    "aloha_set_render_tile",
+    "aloha_composite_over_noalloc", "aloha_set_render_tile",
 ]
 
 
@@ -99,6 +99,7 @@ _SIGS = {
     "aloha_render_batch": ([P, P, I, ctypes.POINTER(P), P], I),
     "aloha_forward": ([P, I, P, I, P], I),
     "aloha_backward": ([P, I, P, P, P, P, P, P], I),
+    "aloha_composite_over_noalloc": ([P, P, I, I, I, I, P, P], I),
     "aloha_set_render_tile": ([P, I, I], I),
 }
 

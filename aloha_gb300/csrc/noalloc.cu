@@ -1,0 +1,93 @@
+// noalloc.cu -- aloha_composite_over_noalloc: the ordered "over" composite
+// without any device allocation.
+//
+// aloha_composite_over stages the composite order in a device buffer it
+// allocates per call (cudaMalloc / cudaFree).  Some callers cannot allocate
+// device memory at that point: a compositing stage called from inside
+// another library's frame loop whose memory pool forbids extra allocations,
+// real-time hosts that ban allocation after start-up, or code that must not
+// synchronize the device (cudaFree does).  This entry point stages the order
+// in a fixed device array that lives in the library instead:
+//
+//   * the array is a file-scope __device__ array of kNoAllocMaxRanks ints
+//     (16 KB); every GPU that loads the library holds it until exit;
+//   * its device address is looked up with cudaGetSymbolAddress once per
+//     device, on the first call made with that device current, so that first
+//     call should come before any stream capture;
+//   * every call on a device shares the one array and overwrites the first
+//     n_ranks entries, so calls whose copies or kernels overlap on the GPU
+//     race; issue them on one stream or wait in between;
+//   * more than kNoAllocMaxRanks ranks is rejected with
+//     ALOHA_ERR_OUT_OF_RANGE.
+//
+// Images and the frame buffer must be device memory (the caller owns them);
+// the order is read from host memory.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
+
+#include "internal.h"
+
+namespace aloha {
+
+constexpr int kNoAllocMaxRanks = 4096;
+constexpr int kNoAllocMaxDevices = 64;
+
+namespace {
+
+__device__ __align__(256) int g_noalloc_order[kNoAllocMaxRanks];
+
+std::mutex g_setup_mutex;
+int* g_order_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_order for the current device (set up once).
+cudaError_t order_scratch(int** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (!g_order_ptr[dev]) {
+    int* p = nullptr;
+    e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_noalloc_order);
+    if (e != cudaSuccess) return e;
+    g_order_ptr[dev] = p;
+  }
+  *out = g_order_ptr[dev];
+  return cudaSuccess;
+}
+
+bool on_device(const void* p) {
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+}  // namespace aloha
+
+extern "C" int aloha_composite_over_noalloc(const float* rank_images, const int* order, int n_ranks, int width,
+                                            int height, int mode, uint32_t* fb, void* stream) {
+  using namespace aloha;
+  if (!rank_images || !order || !fb) return ALOHA_ERR_NULL_POINTER;
+  if (n_ranks < 1 || width < 1 || height < 1 || (long long)width * height > (1ll << 30))
+    return ALOHA_ERR_INVALID_ARGUMENT;
+  if (n_ranks > kNoAllocMaxRanks) return ALOHA_ERR_OUT_OF_RANGE;
+  if (mode != ALOHA_COMPOSITE_FP32 && mode != ALOHA_COMPOSITE_UBYTE) return ALOHA_ERR_INVALID_ARGUMENT;
+  if (!on_device(rank_images) || !on_device(fb) || on_device(order)) return ALOHA_ERR_INVALID_ARGUMENT;
+  for (int k = 0; k < n_ranks; ++k)
+    if (order[k] < 0 || order[k] >= n_ranks) return ALOHA_ERR_OUT_OF_RANGE;
+  int* d_order = nullptr;
+  if (order_scratch(&d_order) != cudaSuccess) return ALOHA_ERR_CUDA;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (cudaMemcpyAsync(d_order, order, sizeof(int) * (size_t)n_ranks, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return ALOHA_ERR_CUDA;
+  if (launch_composite_f32(reinterpret_cast<const float4*>(rank_images), d_order, n_ranks, width * height, mode, fb,
+                           s) != cudaSuccess)
+    return ALOHA_ERR_CUDA;
+  return ALOHA_OK;
+}

@@ -163,6 +163,20 @@ int aloha_composite_over(const float* rank_images, const int* order, int n_ranks
 int aloha_composite_over_rgba8(const uint32_t* rank_fbs, const int* order, int n_ranks, int width, int height,
                                uint32_t* fb, void* stream);
 
+/* The ordered composite of aloha_composite_over for callers that cannot
+ * allocate device memory during the call (for example a compositing stage
+ * inside another library's frame loop whose memory pool forbids new
+ * allocations, or a real-time host that bans allocation after start-up).  No
+ * reference counterpart.  It allocates nothing: the composite order is staged
+ * in a 16 KB device array compiled into the library (held by every GPU that
+ * loads it until exit), whose address is looked up on the first call made on
+ * each device, so that first call should come before any stream capture.
+ * rank_images and fb must be device memory, order host memory; at most 4096
+ * ranks (else ALOHA_ERR_OUT_OF_RANGE).  Calls share the staging array, so
+ * calls that overlap on the GPU race: use one stream or wait in between. */
+int aloha_composite_over_noalloc(const float* rank_images, const int* order, int n_ranks, int width, int height,
+                                 int mode, uint32_t* fb, void* stream);
+
 int aloha_get_stats(aloha_ctx* ctx, aloha_stats* out);
 
 /* ---- Batched form: many views in one persistent launch (no reference
