@@ -79,23 +79,26 @@ __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevVi
     const float mag = fmaxf(fmaxf(fabsf(ray.o[0]) + fabsf(b.lo[0]), fabsf(ray.o[1]) + fabsf(b.lo[1])),
                             fabsf(ray.o[2]) + fabsf(b.lo[2])) + fabsf(t1);
     const float eps = 2e-6f * mag + 1e-4f;
+    float t_cell = t0;  // samples before it lie in a macrocell found non-empty
     while (t < t1 && color.w < a.et_alpha && nb < cap) {
       if (n == max_samples) return n;
       const float ux = fmaf(t, ray.d[0], ray.o[0]) - b.lo[0];
       const float uy = fmaf(t, ray.d[1], ray.o[1]) - b.lo[1];
       const float uz = fmaf(t, ray.d[2], ray.o[2]) - b.lo[2];
-      if (SKIP && b.empty) {
+      if (SKIP && b.empty && !(t < t_cell)) {
         const int mx = min(max((int)floorf(ux), 0), b.n[0] - 1) >> kMacroShift;
         const int my = min(max((int)floorf(uy), 0), b.n[1] - 1) >> kMacroShift;
         const int mz = min(max((int)floorf(uz), 0), b.n[2] - 1) >> kMacroShift;
-        if (__ldg(b.empty + (mz * mny + my) * mnx + mx)) {
-          const float bnd[3] = {(float)(mx << kMacroShift), (float)(my << kMacroShift), (float)(mz << kMacroShift)};
-          float tb = t1;
+        const float bnd[3] = {(float)(mx << kMacroShift), (float)(my << kMacroShift), (float)(mz << kMacroShift)};
+        float tb = t1;
 #pragma unroll
-          for (int ax = 0; ax < 3; ++ax) {
-            const float face = ray.d[ax] > 0.f ? bnd[ax] + (float)kMacro - eps : bnd[ax] + eps;
-            tb = fminf(tb, (face - (ray.o[ax] - b.lo[ax])) * (1.0f / ray.d[ax]));
-          }
+        for (int ax = 0; ax < 3; ++ax) {
+          const float face = ray.d[ax] > 0.f ? bnd[ax] + (float)kMacro - eps : bnd[ax] + eps;
+          tb = fminf(tb, (face - (ray.o[ax] - b.lo[ax])) * (1.0f / ray.d[ax]));
+        }
+        if (!__ldg(b.empty + (mz * mny + my) * mnx + mx)) {
+          t_cell = tb;
+        } else {
           do {
             skipped(t, w, nb, color);
             ++n;
@@ -368,7 +371,6 @@ __global__ void __launch_bounds__(128) backward_kernel(TrainArgs a, int view) {
           const float4 e0 = tf_s[ic + 2], e1 = tf_s[ic + 3];
           const float de[4] = {e1.x - e0.x, e1.y - e0.y, e1.z - e0.z, e1.w - e0.w};
           float dv = 0.f;
-#pragma unroll
           if (i0 != pend_i) {
             flush_tf(dtf_s, a.n_tf, pend_i, pend);
             pend_i = i0;

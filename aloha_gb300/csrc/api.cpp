@@ -122,6 +122,10 @@ struct aloha_ctx {
   // the transfer-function size through shared memory)
   int chunk_w = 0, chunk_h = 0;  // 0 = automatic
   int grid_n_tf = -1, grid_blocks = 0, grid_cw = 0, grid_ch = 0;
+  // rank-split render: mode, scratch rank images, per-chunk tickets, grid
+  int split_mode = ALOHA_SPLIT_AUTO;
+  DeviceBuffer split_images, split_masks, split_items, split_done;
+  int split_grid_n_tf = -1, split_grid_blocks = 0;
   uint64_t last_samples = 0;
   bool samples_valid = false;
 
@@ -152,6 +156,94 @@ void invalidate_training(aloha_ctx* c) {
   for (auto& v : c->views) v.train.valid = false;
 }
 
+// Conservative screen rectangle of every virtual rank, in 8x4-pixel chunks
+// (inclusive [cx0, cy0, cx1, cy1]; cx0 > cx1 when no pixel ray can enter the
+// rank's bricks).  A brick corner P projects to the continuous pixel
+// coordinates (su, sv) solving P - org = a (dir_00 + su du + sv dv); the box
+// projects into the hull of its corners when all of them lie in front of the
+// camera (a > 0), else the rank gets the whole frame.  The margin covers the
+// ray generation's rounding and its clamp of tiny direction components
+// (up to 2e-5 per component of the unit direction).
+std::vector<int> rank_screen_rects(const aloha_ctx* c, const ViewState& v) {
+  const int R = c->n_ranks;
+  const int cxn = (v.width + 7) / 8, cyn = (v.height + 3) / 4;
+  std::vector<double> x0(R, 1e300), y0(R, 1e300), x1(R, -1e300), y1(R, -1e300);
+  std::vector<char> full(R, 0);
+  const double d00[3] = {v.dir_00[0], v.dir_00[1], v.dir_00[2]};
+  const double du[3] = {v.dir_du[0], v.dir_du[1], v.dir_du[2]};
+  const double dv[3] = {v.dir_dv[0], v.dir_dv[1], v.dir_dv[2]};
+  // det [d00 du dv] and the cofactor rows for Cramer's rule
+  auto det3 = [](const double a[3], const double b[3], const double cc[3]) {
+    return a[0] * (b[1] * cc[2] - b[2] * cc[1]) - b[0] * (a[1] * cc[2] - a[2] * cc[1]) +
+           cc[0] * (a[1] * b[2] - a[2] * b[1]);
+  };
+  const double det = det3(d00, du, dv);
+  // angle of one pixel (smallest over the frame corners) for the margin
+  double dmax = 0.0;
+  for (int cy = 0; cy < 2; ++cy)
+    for (int cx = 0; cx < 2; ++cx) {
+      double n2 = 0.0;
+      for (int a = 0; a < 3; ++a) {
+        const double d = d00[a] + cx * v.width * du[a] + cy * v.height * dv[a];
+        n2 += d * d;
+      }
+      dmax = std::max(dmax, std::sqrt(n2));
+    }
+  const double lu = std::sqrt(du[0] * du[0] + du[1] * du[1] + du[2] * du[2]);
+  const double lv = std::sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+  const double pix_angle = dmax > 0.0 ? std::min(lu, lv) / dmax : 0.0;
+  const bool degenerate = !(std::fabs(det) > 1e-30) || !(pix_angle > 1e-12);
+  const double margin = degenerate ? 0.0 : 2.0 + 6e-5 / pix_angle;
+  for (size_t b = 0; b < c->boxes.size(); ++b) {
+    const int r = c->brick_rank[b];
+    if (r < 0 || r >= R || full[r]) continue;
+    if (degenerate) {
+      full[r] = 1;
+      continue;
+    }
+    for (int k = 0; k < 8; ++k) {
+      double rhs[3];
+      for (int a = 0; a < 3; ++a)
+        rhs[a] = (double)((k >> a) & 1 ? c->boxes[b].hi[a] : c->boxes[b].lo[a]) - (double)v.org[a];
+      const double A = det3(rhs, du, dv) / det, B = det3(d00, rhs, dv) / det, C = det3(d00, du, rhs) / det;
+      double scale = 0.0;
+      for (int a = 0; a < 3; ++a) scale = std::max(scale, std::fabs(rhs[a]));
+      if (!(A > 1e-6 * (scale + 1.0) / (dmax + 1e-300))) {
+        full[r] = 1;
+        break;
+      }
+      const double su = B / A - 0.5, sv = C / A - 0.5;  // pixel index whose centre the corner meets
+      x0[r] = std::min(x0[r], su);
+      x1[r] = std::max(x1[r], su);
+      y0[r] = std::min(y0[r], sv);
+      y1[r] = std::max(y1[r], sv);
+    }
+  }
+  std::vector<int> rects(4 * (size_t)R);
+  for (int r = 0; r < R; ++r) {
+    int* q = &rects[4 * (size_t)r];
+    if (full[r]) {
+      q[0] = 0, q[1] = 0, q[2] = cxn - 1, q[3] = cyn - 1;
+      continue;
+    }
+    if (x0[r] > x1[r]) {  // no bricks
+      q[0] = 1, q[1] = 1, q[2] = 0, q[3] = 0;
+      continue;
+    }
+    auto clampd = [](double t, double lo, double hi) { return t < lo ? lo : (t > hi ? hi : t); };
+    const double px0 = clampd(std::floor(x0[r] - margin), -8.0, v.width + 8.0);
+    const double px1 = clampd(std::ceil(x1[r] + margin), -8.0, v.width + 8.0);
+    const double py0 = clampd(std::floor(y0[r] - margin), -8.0, v.height + 8.0);
+    const double py1 = clampd(std::ceil(y1[r] + margin), -8.0, v.height + 8.0);
+    q[0] = std::max(0, (int)std::floor(px0 / 8.0));
+    q[2] = std::min(cxn - 1, (int)std::floor(px1 / 8.0));
+    q[1] = std::max(0, (int)std::floor(py0 / 4.0));
+    q[3] = std::min(cyn - 1, (int)std::floor(py1 / 4.0));
+    if (px1 < 0.0 || py1 < 0.0 || px0 >= v.width || py0 >= v.height) q[0] = 1, q[1] = 1, q[2] = 0, q[3] = 0;
+  }
+  return rects;
+}
+
 // Upload dirty view state (camera, size, schedule) for `view` on `s`.
 int prepare_view(aloha_ctx* c, int view, cudaStream_t s) {
   if (c->descs.empty()) return c->fail(ALOHA_ERR_NOT_READY, "no bricks uploaded");
@@ -169,7 +261,7 @@ int prepare_view(aloha_ctx* c, int view, cudaStream_t s) {
     c->empty_dirty = false;
   }
   const int nb = (int)c->descs.size();
-  const int stride = 2 * c->n_ranks + 1 + nb;
+  const int stride = 2 * c->n_ranks + 1 + nb + 4 * c->n_ranks;
   if (stride != c->sched_stride) {
     CUDA_TRY(c, c->sched_dev.ensure(sizeof(int) * (size_t)stride * kMaxViews));
     c->sched_stride = stride;
@@ -193,7 +285,9 @@ int prepare_view(aloha_ctx* c, int view, cudaStream_t s) {
   slot.insert(slot.end(), order.begin(), order.end());
   slot.insert(slot.end(), v.sched.rank_start.begin(), v.sched.rank_start.end());
   slot.insert(slot.end(), v.sched.rank_bricks.begin(), v.sched.rank_bricks.end());
-  slot.resize(stride, 0);
+  slot.resize(2 * c->n_ranks + 1 + nb, 0);
+  const std::vector<int> rects = rank_screen_rects(c, v);
+  slot.insert(slot.end(), rects.begin(), rects.end());
   DevView dv{};
   for (int a = 0; a < 3; ++a) {
     dv.org[a] = v.org[a];
@@ -217,6 +311,7 @@ int prepare_view(aloha_ctx* c, int view, cudaStream_t s) {
   }
   dv.n_ranks = c->n_ranks;
   dv.sched = view * stride;
+  dv.rects = view * stride + 2 * c->n_ranks + 1 + nb;
   int* sched_dst = static_cast<int*>(c->sched_dev.ptr) + (size_t)view * stride;
   CUDA_TRY(c, cudaMemcpyAsync(sched_dst, slot.data(), sizeof(int) * stride, cudaMemcpyHostToDevice, s));
   CUDA_TRY(c, cudaMemcpyAsync(static_cast<DevView*>(c->views_dev.ptr) + view, &dv, sizeof dv,
@@ -246,15 +341,78 @@ int prepare_accum(aloha_ctx* c, int view, cudaStream_t s, float4** out) {
   return ALOHA_OK;
 }
 
+constexpr size_t kSplitScratchCap = size_t(16) << 30;  // rank split scratch limit
+
+// Bytes of scratch the rank split of `v` needs: rank image planes, masks,
+// item list, tickets.
+size_t split_scratch_bytes(const aloha_ctx* c, const ViewState& v) {
+  const size_t slots = (size_t)ring_slots(v.width, v.height, 8, 4);
+  return (size_t)c->n_ranks * v.width * v.height * sizeof(float4) + slots * (8 + 4 + 4 * (size_t)c->n_ranks);
+}
+
+// The rank split serves aloha_render (a frame buffer, no rank planes wanted)
+// with 1 < n_ranks <= kSplitMaxRanks.
+bool rank_split_possible(const aloha_ctx* c, const FrameArgs& f, const ViewState& v) {
+  return f.fb && !f.rank_images && !f.rank_depth && c->n_ranks >= 2 && c->n_ranks <= kSplitMaxRanks &&
+         ring_slots(v.width, v.height, 8, 4) < (1 << 25);
+}
+
+// Automatic mode keeps the pixel split: on a 512^3 volume in 8 bricks at
+// 1024^2 it measured faster (the longest chunks spend most of their samples
+// inside one brick, so the rank split adds ticket and plane traffic without
+// shortening them).
+bool use_rank_split(const aloha_ctx* c, const FrameArgs& f, const ViewState& v) {
+  return c->split_mode == ALOHA_SPLIT_RANKS && rank_split_possible(c, f, v) &&
+         split_scratch_bytes(c, v) <= kSplitScratchCap;
+}
+
+// Rank-split launch of a single view (mask, plan and render kernels).
+int launch_split(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
+  const ViewState& v = c->views[view];
+  const int R = c->n_ranks;
+  SplitArgs a{};
+  a.f = f;
+  a.view = view;
+  a.n_slots = ring_slots(v.width, v.height, 8, 4);
+  CUDA_TRY(c, c->split_images.ensure((size_t)R * v.width * v.height * sizeof(float4)));
+  a.f.rank_images = static_cast<float4*>(c->split_images.ptr);
+  CUDA_TRY(c, c->split_masks.ensure((size_t)a.n_slots * sizeof(unsigned long long)));
+  a.masks = static_cast<unsigned long long*>(c->split_masks.ptr);
+  CUDA_TRY(c, c->split_items.ensure((size_t)a.n_slots * R * sizeof(uint32_t) + 16));
+  a.items = static_cast<uint32_t*>(c->split_items.ptr);
+  a.n_items = reinterpret_cast<uint32_t*>(static_cast<char*>(c->split_items.ptr) + (size_t)a.n_slots * R * 4);
+  const size_t before = c->split_done.bytes;
+  CUDA_TRY(c, c->split_done.ensure((size_t)a.n_slots * sizeof(unsigned int)));
+  if (c->split_done.bytes != before) CUDA_TRY(c, cudaMemsetAsync(c->split_done.ptr, 0, c->split_done.bytes, s));
+  a.chunk_done = static_cast<unsigned int*>(c->split_done.ptr);
+  a.work_counter = static_cast<unsigned int*>(c->work.ptr);
+  if (c->split_grid_n_tf != c->n_tf) {
+    const int per_sm = render_split_blocks_per_sm(c->n_tf);
+    if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "render occupancy query failed");
+    c->split_grid_blocks = per_sm * c->num_sms;
+    c->split_grid_n_tf = c->n_tf;
+  }
+  CUDA_TRY(c, launch_render_split(a, c->split_grid_blocks, s));
+  return ALOHA_OK;
+}
+
 // One persistent render launch of a single view (resets the work counter).
 int launch_single(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   const ViewState& v = c->views[view];
-  // automatic chunk: 8x8 for large frames, single 8x4 sub-tiles when a frame
-  // has too few chunks to give every resident warp several
+  if (use_rank_split(c, f, v)) return launch_split(c, f, view, s);
+  if (c->split_mode == ALOHA_SPLIT_RANKS && f.fb && !f.rank_images && !f.rank_depth && c->n_ranks > 1) {
+    if (c->n_ranks > kSplitMaxRanks)
+      return c->fail(ALOHA_ERR_UNSUPPORTED, "rank split: %d ranks exceed %d", c->n_ranks, kSplitMaxRanks);
+    if (split_scratch_bytes(c, v) > kSplitScratchCap)
+      return c->fail(ALOHA_ERR_UNSUPPORTED, "rank split: scratch of %zu bytes exceeds 16 GiB", split_scratch_bytes(c, v));
+  }
+  // automatic chunk: single 8x4 sub-tiles.  A frame ends with its slowest
+  // chunk (a few long rays), so the smallest chunk ends it soonest: at 1024^2
+  // on 512^3 in 8 bricks, 8x4 took 1.11 ms and 8x8 1.43 ms.
   int cw = c->chunk_w, ch = c->chunk_h;
   if (cw == 0) {
     cw = 8;
-    ch = (long long)v.width * v.height >= 512ll * 512ll ? 8 : 4;
+    ch = 4;
   }
   if (c->grid_n_tf != c->n_tf || c->grid_cw != cw || c->grid_ch != ch) {
     const int per_sm = render_blocks_per_sm(cw, ch, c->n_tf);
@@ -446,7 +604,8 @@ int aloha_destroy(aloha_ctx* c) {
   }
   for (DeviceBuffer* b : {&c->voxels, &c->bricks_dev, &c->staging_in, &c->tf, &c->views_dev, &c->sched_dev,
                           &c->counter, &c->flag, &c->staging_out, &c->mc_ranges, &c->mc_empty, &c->tf_prefix,
-                          &c->work, &c->grad4})
+                          &c->work, &c->grad4, &c->split_images, &c->split_masks, &c->split_items,
+                          &c->split_done})
     b->release();
   delete c;
   return ALOHA_OK;
@@ -698,6 +857,14 @@ int aloha_set_render_tile(aloha_ctx* c, int tile_w, int tile_h) {
                    tile_h);
   c->chunk_w = tile_w;
   c->chunk_h = tile_h;
+  return ALOHA_OK;
+}
+
+int aloha_set_render_split(aloha_ctx* c, int mode) {
+  if (!c) return ALOHA_ERR_NULL_POINTER;
+  if (mode != ALOHA_SPLIT_AUTO && mode != ALOHA_SPLIT_PIXELS && mode != ALOHA_SPLIT_RANKS)
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "split mode %d not AUTO (0), PIXELS (1) or RANKS (2)", mode);
+  c->split_mode = mode;
   return ALOHA_OK;
 }
 

@@ -44,7 +44,9 @@ struct DevView {
   int sched;          // offset of the view's schedule in the schedule buffer:
                       // [rank_order n_ranks][rank_start n_ranks+1][rank_bricks n_bricks]
   int pixel_offset;   // offset of the view's first pixel in batched outputs
-  int pad[2];
+  int rects;          // offset of the ranks' screen rectangles in the schedule buffer:
+                      // per rank [cx0, cy0, cx1, cy1] in 8x4 chunks, inclusive
+  int pad;
 };
 
 // Everything one render launch needs, passed by value.
@@ -65,7 +67,6 @@ struct FrameArgs {
   float4* rank_images;          // [n_ranks][H*W] or null
   float* rank_depth;            // [n_ranks][H*W] or null
   float4* accum;                // [n_ranks][H*W] or null
-  uint32_t* pixel_samples;      // [H*W] or null
   unsigned long long* counter;  // total samples (atomic) or null
 };
 
@@ -80,6 +81,23 @@ struct BatchArgs {
   int n_items;
   int single_view;
   int total_tiles;           // chunks in the launch
+  unsigned int* work_counter;
+};
+
+// Rank-split render of one view into f.fb: work items are (8x4 chunk, rank)
+// pairs for the ranks whose screen rectangle covers the chunk; f.rank_images
+// is the scratch plane set [n_ranks][H*W] of the marched ranks.  At most
+// kSplitMaxRanks ranks (one mask bit each).
+constexpr int kSplitMaxRanks = 64;
+constexpr uint32_t kSplitBackground = 127u;  // item code of a chunk no rank covers
+struct SplitArgs {
+  FrameArgs f;
+  int view;
+  int n_slots;                     // ring slots of 8x4 chunks (< 2^25)
+  unsigned long long* masks;       // [n_slots] covering ranks per slot
+  uint32_t* items;                 // [n_slots * max(1, n_ranks)] slot << 7 | rank position
+  uint32_t* n_items;               // items listed (written by the plan kernel)
+  unsigned int* chunk_done;        // [n_slots] tickets, zero between launches
   unsigned int* work_counter;
 };
 
@@ -119,5 +137,7 @@ inline int macrocells(const DevBrick& b) {
 }
 // CTAs of the render kernel that fit on one SM for a chunk shape (0 if the shape is unknown).
 int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf);
+cudaError_t launch_render_split(const SplitArgs& a, int grid, cudaStream_t s);
+int render_split_blocks_per_sm(int n_tf);
 
 }  // namespace aloha

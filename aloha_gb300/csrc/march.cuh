@@ -230,25 +230,30 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
   const float eps = 2e-6f * mag + 1e-4f;
   uint32_t n = 0;
   float t = first_sample_t(t0, dt, ils);
+  // Samples before t_cell lie in the last macrocell found non-empty, so they
+  // need no lookup.  Only the skip below depends on the lookup (a full sample
+  // in an empty macrocell leaves the colour unchanged as well), so the bound
+  // only has to be right for speed.
+  float t_cell = t0;
   while (t < t1 && color.w < et && n < cap) {
     const float ux = fmaf(t, r.d[0], r.o[0]) - lox;
     const float uy = fmaf(t, r.d[1], r.o[1]) - loy;
     const float uz = fmaf(t, r.d[2], r.o[2]) - loz;
-    if (empty) {
+    if (empty && !(t < t_cell)) {
       const int mx = min(max((int)floorf(ux), 0), nx - 1) >> kMacroShift;
       const int my = min(max((int)floorf(uy), 0), ny - 1) >> kMacroShift;
       const int mz = min(max((int)floorf(uz), 0), nz - 1) >> kMacroShift;
+      // tb: the ray's exit from the macrocell's box shrunk by eps; every
+      // sample before it lies in this macrocell.
+      const float bx = (float)(mx << kMacroShift), by = (float)(my << kMacroShift), bz = (float)(mz << kMacroShift);
+      const float ex = ((r.d[0] > 0.f ? bx + (float)kMacro - eps : bx + eps) - offx) * idx_;
+      const float ey = ((r.d[1] > 0.f ? by + (float)kMacro - eps : by + eps) - offy) * idy;
+      const float ez = ((r.d[2] > 0.f ? bz + (float)kMacro - eps : bz + eps) - offz) * idz;
+      const float tb = fminf(fminf(fminf(ex, ey), ez), t1);
       if (__ldg(empty + (mz * mny + my) * mnx + mx)) {
         // Empty macrocell: a sample there has alpha exactly 0 and leaves the
         // colour unchanged, so only t and the sample count advance (the same
-        // t += dt sequence as full samples).  Every sample before tb, the
-        // ray's exit from the macrocell's box shrunk by eps, lies in this
-        // macrocell; the exact test resumes after it.
-        const float bx = (float)(mx << kMacroShift), by = (float)(my << kMacroShift), bz = (float)(mz << kMacroShift);
-        const float ex = ((r.d[0] > 0.f ? bx + (float)kMacro - eps : bx + eps) - offx) * idx_;
-        const float ey = ((r.d[1] > 0.f ? by + (float)kMacro - eps : by + eps) - offy) * idy;
-        const float ez = ((r.d[2] > 0.f ? bz + (float)kMacro - eps : bz + eps) - offz) * idz;
-        const float tb = fminf(fminf(fminf(ex, ey), ez), t1);
+        // t += dt sequence as full samples) up to tb; the test resumes there.
         ++n;
         t = t + dt;
         while (t < tb && n < cap) {
@@ -257,6 +262,7 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
         }
         continue;
       }
+      t_cell = tb;
     }
     ++n;
     const StencilOut s = stencil(base, sy, sz, nx, ny, nz, ux, uy, uz);
@@ -299,6 +305,115 @@ __device__ __forceinline__ void load_tf(float4* tf_s, const float4* __restrict__
   }
 }
 
+// One virtual rank's march for one pixel (deviceCode.cpp:378-399): the
+// rank's bricks [j0, j1) of the view schedule front to back, spp draws, early
+// termination on the rank's own alpha.  Returns the spp sum of the colours;
+// z = nearest brick entry / max depth, ns = samples taken.
+__device__ __forceinline__ float4 march_rank(const FrameArgs& a, const DevView& v, const float4* tf_s, const Ray& ray,
+                                             const int* __restrict__ rbricks, int j0, int j1, int pixel, float& z,
+                                             uint32_t& ns) {
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  uint32_t draw = 0;
+  for (int s = 0; s < a.spp; ++s) {
+    float4 color = make_float4(0.f, 0.f, 0.f, 0.f);
+    float tmin = 0.0f;
+    for (int j = j0; j < j1; ++j) {
+      const DevBrick b = a.bricks[__ldg(rbricks + j)];
+      float t0, t1;
+      if (!slab(ray, b.space_lo, b.space_hi, tmin, 1e10f, t0, t1)) continue;
+      const float ils = jitter(a.jitter_mode, a.jitter_value, (uint32_t)pixel, (uint32_t)a.accum_id, draw++);
+      const float tnear = (t0 > tmin ? t0 : 0.0f) + tmin;
+      z = fminf(z, tnear / v.max_depth);
+      ns += march_brick(b, tf_s, a.n_tf, ray, t0, t1, ils, a.dt, a.et_alpha, color);
+      tmin = t1 + 1e-20f;
+      if (!(color.w < a.et_alpha)) break;
+    }
+    acc.x = acc.x + color.x;
+    acc.y = acc.y + color.y;
+    acc.z = acc.z + color.z;
+    acc.w = acc.w + color.w;
+  }
+  return acc;
+}
+
+// renderFrame's per-rank output stage (deviceCode.cpp:400-416): heat map,
+// accumulation buffer, 1/(accumID+1) scale, crosshair, 1/spp.  Writes the
+// rank's image and depth into the given [n_ranks][H*W] planes when they are
+// not null; returns the rank image.
+__device__ __forceinline__ float4 rank_output(const FrameArgs& a, int W, int H, int r, int x, int y, int pixel,
+                                              size_t npx, float4 acc, uint32_t ns, float z, float4* img_planes,
+                                              float* depth_planes) {
+  if (a.heat_map) {
+    float hc[3];
+    heat_color((float)ns * (a.heat_map_scale / (float)a.spp), hc);
+    acc.x = fmaf(0.5f, acc.x, hc[0]);
+    acc.y = fmaf(0.5f, acc.y, hc[1]);
+    acc.z = fmaf(0.5f, acc.z, hc[2]);
+    acc.w = fmaf(0.5f, acc.w, 0.5f);
+  }
+  if (a.accum) {
+    float4* ap = a.accum + ((size_t)r * npx + pixel);
+    if (a.accum_id > 0) {
+      const float4 old = *ap;
+      acc.x = acc.x + old.x;
+      acc.y = acc.y + old.y;
+      acc.z = acc.z + old.z;
+      acc.w = acc.w + old.w;
+    }
+    if (a.accumulate) *ap = acc;
+  }
+  const float scale = 1.0f / (float)(a.accum_id + 1);
+  acc.x = acc.x * scale;
+  acc.y = acc.y * scale;
+  acc.z = acc.z * scale;
+  acc.w = acc.w * scale;
+  if (a.crosshair && (x == W / 2 || y == H / 2)) {
+    acc.x = 1.0f - acc.x;
+    acc.y = 1.0f - acc.y;
+    acc.z = 1.0f - acc.z;
+    acc.w = 1.0f - acc.w;
+  }
+  const float inv_spp = 1.0f / (float)a.spp;
+  const float4 img = make_float4(acc.x * inv_spp, acc.y * inv_spp, acc.z * inv_spp, acc.w * inv_spp);
+  if (img_planes) img_planes[(size_t)r * npx + pixel] = img;
+  if (depth_planes) depth_planes[(size_t)r * npx + pixel] = z;
+  return img;
+}
+
+// Front-to-back ordered "over" of rank images (IceT BLEND with
+// ORDERED_COMPOSITE, waikikiRenderer.cpp:910-917,1042-1079): in fp32, or on
+// images quantised to 8 bits per channel like IceT's RGBA_UBYTE buffers.
+struct OverBlend {
+  float4 comp = make_float4(0.f, 0.f, 0.f, 0.f);
+  uint32_t c8[4] = {0u, 0u, 0u, 0u};
+  __device__ __forceinline__ void add(int mode, float4 img) {
+    if (mode == ALOHA_COMPOSITE_UBYTE) {
+      const uint32_t q0 = quantize8(img.x), q1 = quantize8(img.y), q2 = quantize8(img.z), q3 = quantize8(img.w);
+      const uint32_t f = 255u - c8[3];
+      c8[0] = min(255u, c8[0] + (q0 * f + 127u) / 255u);
+      c8[1] = min(255u, c8[1] + (q1 * f + 127u) / 255u);
+      c8[2] = min(255u, c8[2] + (q2 * f + 127u) / 255u);
+      c8[3] = min(255u, c8[3] + (q3 * f + 127u) / 255u);
+    } else {
+      const float oma = 1.0f - comp.w;
+      comp.x = fmaf(oma, img.x, comp.x);
+      comp.y = fmaf(oma, img.y, comp.y);
+      comp.z = fmaf(oma, img.z, comp.z);
+      comp.w = fmaf(oma, img.w, comp.w);
+    }
+  }
+  __device__ __forceinline__ uint32_t pack(int mode) const {
+    return mode == ALOHA_COMPOSITE_UBYTE ? (c8[0] | (c8[1] << 8) | (c8[2] << 16) | (c8[3] << 24)) : pack_rgba(comp);
+  }
+};
+
+// Island membership of a pixel (16x16 tiles dealt round-robin).
+__device__ __forceinline__ bool pixel_in_island(const FrameArgs& a, int W, int x, int y) {
+  if (a.num_islands <= 1) return true;
+  const int tiles_x = (W + 15) / 16;
+  return (((x >> 4) + tiles_x * (y >> 4)) % a.num_islands) == a.island_id;
+}
+
 // One pixel of one view: every virtual rank marches its bricks and runs
 // renderFrame's output stage; the rank images are blended front to back.
 // Returns the number of samples.
@@ -311,99 +426,20 @@ __device__ __forceinline__ uint32_t render_pixel(const FrameArgs& a, const DevVi
   const int* __restrict__ order = a.sched + v.sched;
   const int* __restrict__ rstart = order + R;
   const int* __restrict__ rbricks = rstart + R + 1;
-  bool in_island = true;
-  if (a.num_islands > 1) {
-    const int tiles_x = (W + 15) / 16;
-    in_island = (((x >> 4) + tiles_x * (y >> 4)) % a.num_islands) == a.island_id;
-  }
+  const bool in_island = pixel_in_island(a, W, x, y);
   const Ray ray = generate_ray(v, x, y);
-  float4 comp = make_float4(0.f, 0.f, 0.f, 0.f);
-  uint32_t comp8[4] = {0u, 0u, 0u, 0u};
+  OverBlend blend;
   uint32_t total = 0;
   for (int k = 0; k < R; ++k) {
     const int r = __ldg(order + k);
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     float z = 1.0f;
     uint32_t ns = 0;
-    if (in_island) {
-      uint32_t draw = 0;
-      const int j0 = __ldg(rstart + r), j1 = __ldg(rstart + r + 1);
-      for (int s = 0; s < a.spp; ++s) {
-        float4 color = make_float4(0.f, 0.f, 0.f, 0.f);
-        float tmin = 0.0f;
-        for (int j = j0; j < j1; ++j) {
-          const DevBrick b = a.bricks[__ldg(rbricks + j)];
-          float t0, t1;
-          if (!slab(ray, b.space_lo, b.space_hi, tmin, 1e10f, t0, t1)) continue;
-          const float ils = jitter(a.jitter_mode, a.jitter_value, (uint32_t)pixel, (uint32_t)a.accum_id, draw++);
-          const float tnear = (t0 > tmin ? t0 : 0.0f) + tmin;
-          z = fminf(z, tnear / v.max_depth);
-          ns += march_brick(b, tf_s, a.n_tf, ray, t0, t1, ils, a.dt, a.et_alpha, color);
-          tmin = t1 + 1e-20f;
-          if (!(color.w < a.et_alpha)) break;
-        }
-        acc.x = acc.x + color.x;
-        acc.y = acc.y + color.y;
-        acc.z = acc.z + color.z;
-        acc.w = acc.w + color.w;
-      }
-    }
-    if (a.heat_map) {
-      float hc[3];
-      heat_color((float)ns * (a.heat_map_scale / (float)a.spp), hc);
-      acc.x = fmaf(0.5f, acc.x, hc[0]);
-      acc.y = fmaf(0.5f, acc.y, hc[1]);
-      acc.z = fmaf(0.5f, acc.z, hc[2]);
-      acc.w = fmaf(0.5f, acc.w, 0.5f);
-    }
-    if (a.accum) {
-      float4* ap = a.accum + ((size_t)r * npx + pixel);
-      if (a.accum_id > 0) {
-        const float4 old = *ap;
-        acc.x = acc.x + old.x;
-        acc.y = acc.y + old.y;
-        acc.z = acc.z + old.z;
-        acc.w = acc.w + old.w;
-      }
-      if (a.accumulate) *ap = acc;
-    }
-    const float scale = 1.0f / (float)(a.accum_id + 1);
-    acc.x = acc.x * scale;
-    acc.y = acc.y * scale;
-    acc.z = acc.z * scale;
-    acc.w = acc.w * scale;
-    if (a.crosshair && (x == W / 2 || y == H / 2)) {
-      acc.x = 1.0f - acc.x;
-      acc.y = 1.0f - acc.y;
-      acc.z = 1.0f - acc.z;
-      acc.w = 1.0f - acc.w;
-    }
-    const float inv_spp = 1.0f / (float)a.spp;
-    const float4 img = make_float4(acc.x * inv_spp, acc.y * inv_spp, acc.z * inv_spp, acc.w * inv_spp);
-    if (a.rank_images) a.rank_images[(size_t)r * npx + pixel] = img;
-    if (a.rank_depth) a.rank_depth[(size_t)r * npx + pixel] = z;
-    if (a.composite_mode == ALOHA_COMPOSITE_UBYTE) {
-      const uint32_t q0 = quantize8(img.x), q1 = quantize8(img.y), q2 = quantize8(img.z), q3 = quantize8(img.w);
-      const uint32_t f = 255u - comp8[3];
-      comp8[0] = min(255u, comp8[0] + (q0 * f + 127u) / 255u);
-      comp8[1] = min(255u, comp8[1] + (q1 * f + 127u) / 255u);
-      comp8[2] = min(255u, comp8[2] + (q2 * f + 127u) / 255u);
-      comp8[3] = min(255u, comp8[3] + (q3 * f + 127u) / 255u);
-    } else {
-      const float oma = 1.0f - comp.w;
-      comp.x = fmaf(oma, img.x, comp.x);
-      comp.y = fmaf(oma, img.y, comp.y);
-      comp.z = fmaf(oma, img.z, comp.z);
-      comp.w = fmaf(oma, img.w, comp.w);
-    }
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (in_island) acc = march_rank(a, v, tf_s, ray, rbricks, __ldg(rstart + r), __ldg(rstart + r + 1), pixel, z, ns);
+    blend.add(a.composite_mode, rank_output(a, W, H, r, x, y, pixel, npx, acc, ns, z, a.rank_images, a.rank_depth));
     total += ns;
   }
-  if (fb_out) {
-    fb_out[fb_index] = (a.composite_mode == ALOHA_COMPOSITE_UBYTE)
-                           ? (comp8[0] | (comp8[1] << 8) | (comp8[2] << 16) | (comp8[3] << 24))
-                           : pack_rgba(comp);
-  }
-  if (a.pixel_samples) a.pixel_samples[pixel] = total;
+  if (fb_out) fb_out[fb_index] = blend.pack(a.composite_mode);
   return total;
 }
 

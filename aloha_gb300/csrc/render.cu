@@ -58,33 +58,172 @@ __global__ void __launch_bounds__(kRenderThreads, 6) render_warps_kernel(BatchAr
   count_samples(b.f.counter, n);
 }
 
+// ---- Rank-split render of one view -------------------------------------
+// A work item is one 8x4-pixel chunk for one virtual rank, so the bricks along
+// a pixel's ray are marched by different warps at the same time.  The ranks
+// of a pixel never interact before the composite (each has its own
+// accumulator and early termination, like the reference's one process per
+// rank), so this is render_pixel's arithmetic in another schedule.
+//
+// split_mask_kernel marks, per chunk slot, the ranks whose screen rectangle
+// covers the chunk (bit k = k-th rank in visibility order); no pixel ray of
+// an unmarked rank can enter its bricks, so its image is the output stage of
+// an empty march.  split_plan_kernel lists the work items in slot order
+// (centre-out): one per marked rank, or one compositing-only item for a chunk
+// no rank covers.  render_split_kernel marches each item's rank into its
+// image plane; the warp that completes a chunk's last marked rank (a ticket
+// per chunk, taken after a fence) blends the chunk front to back, evaluating
+// the unmarked ranks' images in place, and resets the ticket for the next
+// launch.  No warp waits on another.
+
+__device__ __forceinline__ bool rect_covers(const int* __restrict__ q, int cx, int cy) {
+  return cx >= __ldg(q) && cy >= __ldg(q + 1) && cx <= __ldg(q + 2) && cy <= __ldg(q + 3);
+}
+
+__global__ void split_mask_kernel(SplitArgs s) {
+  const DevView& v = s.f.views[s.view];
+  const int W = v.width, H = v.height, R = v.n_ranks;
+  const int* __restrict__ order = s.f.sched + v.sched;
+  const int* __restrict__ rects = s.f.sched + v.rects;
+  const int cxn = (W + 7) / 8, cyn = (H + 3) / 4;
+  for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < s.n_slots; slot += gridDim.x * blockDim.x) {
+    int cx, cy;
+    unsigned long long m = 0ull;
+    if (ring_chunk(slot, cxn, cyn, cx, cy))
+      for (int k = 0; k < R; ++k)
+        if (rect_covers(rects + 4 * __ldg(order + k), cx, cy)) m |= 1ull << k;
+    s.masks[slot] = m;
+  }
+}
+
+constexpr int kPlanThreads = 1024;
+
+__device__ __forceinline__ uint32_t slot_items(int slot, int cxn, int cyn, unsigned long long m) {
+  int cx, cy;
+  if (!ring_chunk(slot, cxn, cyn, cx, cy)) return 0u;
+  return m ? (uint32_t)__popcll(m) : 1u;
+}
+
+__global__ void __launch_bounds__(kPlanThreads) split_plan_kernel(SplitArgs s) {
+  __shared__ uint32_t warp_sum[kPlanThreads / 32];
+  const DevView& v = s.f.views[s.view];
+  const int cxn = (v.width + 7) / 8, cyn = (v.height + 3) / 4;
+  const int per = (s.n_slots + kPlanThreads - 1) / kPlanThreads;
+  const int lo = min(s.n_slots, (int)threadIdx.x * per), hi = min(s.n_slots, lo + per);
+  uint32_t count = 0;
+  for (int slot = lo; slot < hi; ++slot) count += slot_items(slot, cxn, cyn, s.masks[slot]);
+  // exclusive block scan of the per-thread counts
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t incl = count;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += o;
+  }
+  if (lane == 31) warp_sum[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t w = warp_sum[lane];
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t o = __shfl_up_sync(0xffffffffu, w, d);
+      if (lane >= d) w += o;
+    }
+    warp_sum[lane] = w;  // inclusive over warps
+  }
+  __syncthreads();
+  uint32_t at = incl - count + (wid > 0 ? warp_sum[wid - 1] : 0u);
+  for (int slot = lo; slot < hi; ++slot) {
+    int cx, cy;
+    if (!ring_chunk(slot, cxn, cyn, cx, cy)) continue;
+    unsigned long long m = s.masks[slot];
+    const uint32_t base = (uint32_t)slot << 7;
+    if (!m) {
+      s.items[at++] = base | kSplitBackground;
+      continue;
+    }
+    while (m) {
+      const int k = __ffsll((long long)m) - 1;
+      m &= m - 1ull;
+      s.items[at++] = base | (uint32_t)k;
+    }
+  }
+  if (threadIdx.x == kPlanThreads - 1) *s.n_items = at;
+}
+
+__global__ void __launch_bounds__(kRenderThreads, 6) render_split_kernel(SplitArgs s) {
+  extern __shared__ float4 tf_s[];
+  load_tf(tf_s, s.f.tf, s.f.n_tf);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int W = s.f.views[s.view].width, H = s.f.views[s.view].height, R = s.f.views[s.view].n_ranks;
+  const size_t npx = (size_t)W * H;
+  const int* __restrict__ order = s.f.sched + s.f.views[s.view].sched;
+  const int* __restrict__ rstart = order + R;
+  const int* __restrict__ rbricks = rstart + R + 1;
+  const int cxn = (W + 7) / 8, cyn = (H + 3) / 4;
+  const uint32_t n_items = *s.n_items;
+  float4* __restrict__ planes = s.f.rank_images;
+  uint32_t n = 0;
+  for (;;) {
+    uint32_t item = 0;
+    if (lane == 0) item = atomicAdd(s.work_counter, 1u);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= n_items) break;
+    const uint32_t code = __ldg(s.items + item);
+    const int slot = (int)(code >> 7), k = (int)(code & 127u);
+    int cx, cy;
+    ring_chunk(slot, cxn, cyn, cx, cy);
+    const int x = cx * 8 + (lane & 7), y = cy * 4 + (lane >> 3);
+    const bool valid = x < W && y < H;
+    const int pixel = x + W * y;
+    const unsigned long long mask = __ldg(s.masks + slot);
+    if (k != kSplitBackground) {
+      if (valid) {
+        const DevView v = s.f.views[s.view];
+        const int r = __ldg(order + k);
+        float z = 1.0f;
+        uint32_t ns = 0;
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (pixel_in_island(s.f, W, x, y))
+          acc = march_rank(s.f, v, tf_s, generate_ray(v, x, y), rbricks, __ldg(rstart + r), __ldg(rstart + r + 1),
+                           pixel, z, ns);
+        rank_output(s.f, W, H, r, x, y, pixel, npx, acc, ns, z, planes, nullptr);
+        n += ns;
+      }
+      __threadfence();
+      __syncwarp();
+      unsigned ticket = 0;
+      if (lane == 0) ticket = atomicAdd(s.chunk_done + slot, 1u);
+      ticket = __shfl_sync(0xffffffffu, ticket, 0);
+      if (ticket != (unsigned)(__popcll(mask) - 1)) continue;
+      __threadfence();
+    }
+    if (valid) {
+      OverBlend blend;
+      for (int kk = 0; kk < R; ++kk) {
+        const int r = __ldg(order + kk);
+        const float4 img = (mask >> kk) & 1ull
+                               ? __ldcg(planes + (size_t)r * npx + pixel)
+                               : rank_output(s.f, W, H, r, x, y, pixel, npx, make_float4(0.f, 0.f, 0.f, 0.f), 0u,
+                                             1.0f, nullptr, nullptr);
+        blend.add(s.f.composite_mode, img);
+      }
+      s.f.fb[pixel] = blend.pack(s.f.composite_mode);
+    }
+    if (lane == 0 && k != kSplitBackground) s.chunk_done[slot] = 0u;
+  }
+  count_samples(s.f.counter, n);
+}
+
 // Ordered "over" of per-rank float images (IceT BLEND with ORDERED_COMPOSITE,
 // waikikiRenderer.cpp:910-917,1042-1079), front to back.
 __global__ void composite_f32_kernel(const float4* __restrict__ imgs, const int* __restrict__ order, int n_ranks,
                                      int npx, int mode, uint32_t* __restrict__ fb) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npx; p += gridDim.x * blockDim.x) {
-    float4 comp = make_float4(0.f, 0.f, 0.f, 0.f);
-    uint32_t c8[4] = {0u, 0u, 0u, 0u};
-    for (int k = 0; k < n_ranks; ++k) {
-      const int r = __ldg(order + k);
-      const float4 img = __ldg(imgs + (size_t)r * npx + p);
-      if (mode == ALOHA_COMPOSITE_UBYTE) {
-        const uint32_t q0 = quantize8(img.x), q1 = quantize8(img.y), q2 = quantize8(img.z), q3 = quantize8(img.w);
-        const uint32_t f = 255u - c8[3];
-        c8[0] = min(255u, c8[0] + (q0 * f + 127u) / 255u);
-        c8[1] = min(255u, c8[1] + (q1 * f + 127u) / 255u);
-        c8[2] = min(255u, c8[2] + (q2 * f + 127u) / 255u);
-        c8[3] = min(255u, c8[3] + (q3 * f + 127u) / 255u);
-      } else {
-        const float oma = 1.0f - comp.w;
-        comp.x = fmaf(oma, img.x, comp.x);
-        comp.y = fmaf(oma, img.y, comp.y);
-        comp.z = fmaf(oma, img.z, comp.z);
-        comp.w = fmaf(oma, img.w, comp.w);
-      }
-    }
-    fb[p] = (mode == ALOHA_COMPOSITE_UBYTE) ? (c8[0] | (c8[1] << 8) | (c8[2] << 16) | (c8[3] << 24))
-                                            : pack_rgba(comp);
+    OverBlend blend;
+    for (int k = 0; k < n_ranks; ++k) blend.add(mode, __ldg(imgs + (size_t)__ldg(order + k) * npx + p));
+    fb[p] = blend.pack(mode);
   }
 }
 
@@ -213,6 +352,27 @@ int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf) {
   else if (chunk_w == 32 && chunk_h == 4)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_warps_kernel<32, 4>, kRenderThreads, smem);
   if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+cudaError_t launch_render_split(const SplitArgs& a, int grid, cudaStream_t s) {
+  int mg = (a.n_slots + 255) / 256;
+  mg = mg < 1 ? 1 : (mg > 152 * 8 ? 152 * 8 : mg);
+  split_mask_kernel<<<mg, 256, 0, s>>>(a);
+  split_plan_kernel<<<1, kPlanThreads, 0, s>>>(a);
+  cudaError_t e = cudaMemsetAsync(a.work_counter, 0, sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
+  render_split_kernel<<<grid, kRenderThreads, tf_smem(a.f.n_tf), s>>>(a);
+  return cudaGetLastError();
+}
+
+int render_split_blocks_per_sm(int n_tf) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_split_kernel, kRenderThreads, tf_smem(n_tf)) !=
+      cudaSuccess) {
     cudaGetLastError();
     return 0;
   }

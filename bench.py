@@ -301,9 +301,13 @@ def main():
             samples_of[ci] = ctx.stats().samples
             bytes_of[ci] = algorithmic_bytes(descs, bricks_hit(descs, cams[ci], W, H), tf.shape[0], W, H)
 
-    # ray-tile sweep of the persistent single-view render (untimed)
-    tile_ms = {}
-    for tw, th in ((8, 8), (16, 8), (32, 4)):
+    # work-division sweep of the single-view render (untimed): the pixel split
+    # at three chunk shapes, and the (chunk, rank) split
+    schedules = {"pixels 8x4": (abi.SPLIT_PIXELS, 8, 4), "pixels 8x8": (abi.SPLIT_PIXELS, 8, 8),
+                 "pixels 16x8": (abi.SPLIT_PIXELS, 16, 8), "ranks": (abi.SPLIT_RANKS, 0, 0)}
+    sched_ms = {}
+    for name, (split, tw, th) in schedules.items():
+        ctx.set_render_split(split)
         ctx.set_render_tile(tw, th)
         probe = mine[:8]
         for ci in probe[:2]:
@@ -318,9 +322,12 @@ def main():
             e1.record(stream)
             e1.synchronize()
             ms += e0.elapsed_time(e1)
-        tile_ms[f"{tw}x{th}"] = ms / len(probe)
-    best_tile = min(tile_ms, key=tile_ms.get)
-    ctx.set_render_tile(*(int(v) for v in best_tile.split("x")))
+        sched_ms[name] = ms / len(probe)
+    best = min(sched_ms, key=sched_ms.get)
+    split, tw, th = schedules[best]
+    ctx.set_render_split(split)
+    ctx.set_render_tile(tw, th)
+    kernel = "render_split_kernel" if split == abi.SPLIT_RANKS else f"render_warps_kernel<{tw},{th}>"
 
     steps = [mine[k % len(mine)] for k in range(args.steps)]
     for k in range(args.warmup):
@@ -351,7 +358,7 @@ def main():
     mean_launch = float(np.mean(launch_ms))
     peak, peak_kind = measured_peaks()
     achieved = mean_bytes / (mean_launch * 1e-3) / 1e9
-    traffic = profile_traffic("render_warps_kernel")
+    traffic = profile_traffic(kernel.split("<")[0])
 
     result = {"metric": METRIC, "value": value, "unit": "Gsamples/s", "n_gpus": world, "steps": args.steps,
               "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
@@ -365,8 +372,7 @@ def main():
               "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                            "frac": achieved / peak, "peak_kind": peak_kind,
                            "traffic": traffic["bytes_per_launch"] if traffic else None,
-                           "kernel": f"render_warps_kernel<{best_tile.replace('x', ',')}>",
-                           "tile_sweep_ms": tile_ms,
+                           "kernel": kernel, "schedule": best, "schedule_sweep_ms": sched_ms,
                            "algorithmic_bytes_per_launch": mean_bytes, "launch_ms": mean_launch}}
     clocks = clk.summary()
     if clocks:

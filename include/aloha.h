@@ -46,6 +46,7 @@ typedef enum {
 enum { ALOHA_JITTER_NONE = 0, ALOHA_JITTER_CONST = 1, ALOHA_JITTER_HASH = 2 };
 enum { ALOHA_COMPOSITE_FP32 = 0, ALOHA_COMPOSITE_UBYTE = 1 };
 enum { ALOHA_ORDER_FACES = 0, ALOHA_ORDER_REFERENCE_KD = 1 };
+enum { ALOHA_SPLIT_AUTO = 0, ALOHA_SPLIT_PIXELS = 1, ALOHA_SPLIT_RANKS = 2 };
 
 typedef struct aloha_ctx aloha_ctx;
 
@@ -135,10 +136,23 @@ int aloha_resize(aloha_ctx* ctx, int view, int width, int height);
 int aloha_get_composite_order(aloha_ctx* ctx, int view, int* rank_order, int max_ranks, int* n_ranks);
 
 /* Pixel chunk a warp of the persistent render takes per grab (rendered as
- * 8x4-pixel sub-tiles): 8x4, 8x8, 16x8 or 32x4; 0x0 (the default) picks 8x8
- * for frames of 512^2 pixels or more and 8x4 below.  No reference
+ * 8x4-pixel sub-tiles): 8x4, 8x8, 16x8 or 32x4; 0x0 (the default) is 8x4,
+ * which ends a frame soonest after its slowest chunk.  No reference
  * counterpart (the raygen launches one thread per pixel). */
 int aloha_set_render_tile(aloha_ctx* ctx, int tile_w, int tile_h);
+
+/* How aloha_render divides a frame among warps.  ALOHA_SPLIT_PIXELS: one
+ * thread marches every virtual rank of its pixel and blends them (the chunk
+ * shape above applies).  ALOHA_SPLIT_RANKS: a work item is one 8x4-pixel
+ * chunk of one rank whose projected bricks cover the chunk, so the bricks
+ * along a ray are marched in parallel; rank images go through a scratch plane
+ * set of n_ranks*width*height float4 and the last rank of each chunk blends
+ * it.  Both give bit-identical frames.  The rank split needs 2..64 virtual
+ * ranks and at most 16 GiB of scratch (else ALOHA_ERR_UNSUPPORTED);
+ * aloha_render_partials and a single rank always use the pixel split.
+ * ALOHA_SPLIT_AUTO (the default) is the pixel split.  No reference
+ * counterpart (each reference rank is its own process). */
+int aloha_set_render_split(aloha_ctx* ctx, int mode);
 
 /* Render one view into an RGBA8 frame buffer of width*height uint32
  * (Renderer::render, waikikiRenderer.cpp:1015-1080): all virtual ranks march

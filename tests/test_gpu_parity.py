@@ -14,6 +14,11 @@ from tests import scenes_for_tests as T
 pytestmark = pytest.mark.gpu
 
 
+# both work divisions of a frame: every parity test below that renders
+# several virtual ranks runs under each
+SPLITS = [abi.SPLIT_PIXELS, abi.SPLIT_RANKS]
+
+
 def setup_ctx(make, descs, vox, tf, n_ranks=None, **params):
     ctx = make()
     ctx.set_bricks(descs, vox)
@@ -54,10 +59,12 @@ def test_plain_c1_bit_exact(gpu_ctx_factory, oracle):
     assert (fb != 0).mean() > 0.1
 
 
-def test_partials_depth_bit_exact(gpu_ctx_factory, oracle):
+@pytest.mark.parametrize("split", SPLITS)
+def test_partials_depth_bit_exact(gpu_ctx_factory, oracle, split):
     vol, descs, vox, tf = T.chopsuey_scene(48, 8)
     W, H = 72, 56
     ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8)
+    ctx.set_render_split(split)
     for cam in T.cameras((48, 48, 48), 3, W, H, seed=21):
         ctx.set_camera(0, *cam)
         ctx.resize(0, W, H)
@@ -72,10 +79,12 @@ def test_partials_depth_bit_exact(gpu_ctx_factory, oracle):
 
 @pytest.mark.parametrize("mode", [abi.COMPOSITE_FP32, abi.COMPOSITE_UBYTE])
 @pytest.mark.parametrize("n_ranks", [1, 2, 3, 8])
-def test_virtual_ranks_bit_exact(gpu_ctx_factory, oracle, mode, n_ranks):
+@pytest.mark.parametrize("split", SPLITS)
+def test_virtual_ranks_bit_exact(gpu_ctx_factory, oracle, mode, n_ranks, split):
     vol, descs, vox, tf = T.chopsuey_scene(64, 8)
     W, H = 100, 76  # not a multiple of the ray tile
     ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=n_ranks, composite_mode=mode)
+    ctx.set_render_split(split)
     for cam in T.cameras((64, 64, 64), 3, W, H, seed=n_ranks):
         fb, samples = gpu_frame(ctx, cam, W, H)
         ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=n_ranks, composite_mode=mode)
@@ -89,6 +98,7 @@ def test_render_tiles_bit_exact(gpu_ctx_factory, oracle, tile):
     vol, descs, vox, tf = T.chopsuey_scene(48, 8)
     W, H = 70, 42  # ragged against every tile shape
     ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8)
+    ctx.set_render_split(abi.SPLIT_PIXELS)  # chunk shapes apply to the pixel split
     ctx.set_render_tile(*tile)
     for cam in T.cameras((48, 48, 48), 2, W, H, seed=61):
         fb, samples = gpu_frame(ctx, cam, W, H)
@@ -97,6 +107,63 @@ def test_render_tiles_bit_exact(gpu_ctx_factory, oracle, tile):
         assert samples == ref["samples"]
     with pytest.raises(abi.AlohaError):
         ctx.set_render_tile(4, 4)
+    with pytest.raises(abi.AlohaError):
+        ctx.set_render_split(3)
+
+
+def _camera_zoo(dims, W, H, seed):
+    """Cameras that stress the rank split's screen rectangles: near, inside,
+    grazing, far with a narrow field of view, off-centre targets."""
+    rng = np.random.default_rng(seed)
+    ext = float(max(dims))
+    ctr = np.asarray(dims, np.float64) * 0.5
+    cams = []
+    for dist, fov in [(0.3, 90.0), (0.55, 70.0), (0.75, 60.0), (1.0, 45.0), (2.0, 30.0), (8.0, 4.0), (60.0, 0.4)]:
+        for _ in range(3):
+            d = rng.normal(size=3)
+            d /= np.linalg.norm(d)
+            org = ctr + d * dist * ext
+            target = ctr + rng.uniform(-0.4, 0.4, size=3) * ext
+            up = rng.normal(size=3)
+            cams.append(S.look_at_camera(org, target, up, fov, W, H))
+    return cams
+
+
+@pytest.mark.parametrize("scene", ["chopsuey8", "uneven12"])
+def test_rank_split_matches_pixel_split(gpu_ctx_factory, scene):
+    """The rank split skips the ranks whose screen rectangle misses a chunk;
+    over many awkward cameras its frames must equal the pixel split's."""
+    if scene == "chopsuey8":
+        vol, descs, vox, tf = T.chopsuey_scene(48, 8)
+        R = 8
+    else:
+        vol, descs, vox, tf = T.uneven_scene(48)
+        R = 12
+    W, H = 61, 45
+    params = [dict(), dict(heat_map=1, heat_map_scale=0.02), dict(crosshair=1, composite_mode=abi.COMPOSITE_UBYTE)]
+    for kw in params:
+        ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=R, **kw)
+        for cam in _camera_zoo((48, 48, 48), W, H, seed=len(kw)):
+            ctx.set_render_split(abi.SPLIT_PIXELS)
+            want, n_want = gpu_frame(ctx, cam, W, H)
+            ctx.set_render_split(abi.SPLIT_RANKS)
+            got, n_got = gpu_frame(ctx, cam, W, H)
+            assert_same_fb(got, want)
+            assert n_got == n_want
+
+
+def test_rank_split_across_resizes(gpu_ctx_factory, oracle):
+    """The per-chunk tickets of the rank split are reset by the kernel itself;
+    frames of growing and shrinking size in a row must all stay exact."""
+    vol, descs, vox, tf = T.chopsuey_scene(48, 8)
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8)
+    ctx.set_render_split(abi.SPLIT_RANKS)
+    for (W, H), seed in [((40, 24), 1), ((130, 70), 2), ((40, 24), 3), ((33, 97), 4)]:
+        cam = T.cameras((48, 48, 48), 1, W, H, seed=seed)[0]
+        fb, samples = gpu_frame(ctx, cam, W, H)
+        ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=8)
+        assert_same_fb(fb, ref["fb"])
+        assert samples == ref["samples"]
 
 
 def test_uneven_bricks_bit_exact(gpu_ctx_factory, oracle):
@@ -131,22 +198,26 @@ def test_reference_kd_order_mode(gpu_ctx_factory, oracle):
     dict(dt=0.25, et_alpha=0.5),
     dict(accum_id=0, crosshair=1, spp=2, composite_mode=abi.COMPOSITE_UBYTE),
 ])
-def test_output_stage_options(gpu_ctx_factory, oracle, kw):
+@pytest.mark.parametrize("split", SPLITS)
+def test_output_stage_options(gpu_ctx_factory, oracle, kw, split):
     vol, descs, vox, tf = T.chopsuey_scene(48, 4)
     W, H = 80, 64
     cam = T.cameras((48, 48, 48), 1, W, H, seed=13)[0]
     ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=4, **kw)
+    ctx.set_render_split(split)
     fb, samples = gpu_frame(ctx, cam, W, H)
     ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=4, **kw)
     assert_same_fb(fb, ref["fb"])
     assert samples == ref["samples"]
 
 
-def test_progressive_accumulation(gpu_ctx_factory, oracle):
+@pytest.mark.parametrize("split", SPLITS)
+def test_progressive_accumulation(gpu_ctx_factory, oracle, split):
     vol, descs, vox, tf = T.chopsuey_scene(48, 2)
     W, H = 64, 48
     cam = T.cameras((48, 48, 48), 1, W, H, seed=17)[0]
     ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=2)
+    ctx.set_render_split(split)
     ctx.set_camera(0, *cam)
     ctx.resize(0, W, H)
     acc = np.zeros((2, W * H, 4), np.float32)
@@ -158,10 +229,12 @@ def test_progressive_accumulation(gpu_ctx_factory, oracle):
         assert_same_fb(fb, ref["fb"])
 
 
-def test_pathological_cameras(gpu_ctx_factory, oracle):
+@pytest.mark.parametrize("split", SPLITS)
+def test_pathological_cameras(gpu_ctx_factory, oracle, split):
     vol, descs, vox, tf = T.chopsuey_scene(32, 8)
     W, H = 40, 40
     ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8)
+    ctx.set_render_split(split)
     cams = [
         S.look_at_camera([16.0, 16.0, 16.0], [40.0, 17.0, 15.0], [0, 1, 0], 60.0, W, H),  # inside, on a face
         S.look_at_camera([16.3, 5.0, 9.0], [16.3, 5.0, -30.0], [0, 1, 0], 30.0, W, H),   # axis-aligned rays
