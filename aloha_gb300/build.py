@@ -71,7 +71,7 @@ def build(force: bool = False, verbose_ptxas: bool = False, jobs: int | None = N
                 sys.stderr.write(r.stdout + r.stderr)
                 raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if todo or not os.path.exists(LIB):
-        link = [cc, "-shared", "-o", LIB] + objs + ARCH
+        link = [cc, "-shared", "-o", LIB] + objs + ARCH + ["-Xlinker", "--no-undefined", "-lcudart"]
         r = subprocess.run(link, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

@@ -415,7 +415,7 @@ int launch_single(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
     ch = 4;
   }
   if (c->grid_n_tf != c->n_tf || c->grid_cw != cw || c->grid_ch != ch) {
-    const int per_sm = render_blocks_per_sm(cw, ch, c->n_tf);
+    const int per_sm = render_blocks_per_sm(cw, ch, c->n_tf, false);
     if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "render occupancy query failed");
     c->grid_blocks = per_sm * c->num_sms;
     c->grid_n_tf = c->n_tf;
@@ -431,7 +431,7 @@ int launch_single(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   const int warps_per_block = kRenderThreads / 32;
   const int grid = std::max(1, std::min(c->grid_blocks, (b.total_tiles + warps_per_block - 1) / warps_per_block));
   CUDA_TRY(c, cudaMemsetAsync(c->work.ptr, 0, sizeof(unsigned int), s));
-  CUDA_TRY(c, launch_render_warps(b, cw, ch, grid, s));
+  CUDA_TRY(c, launch_render_warps(b, cw, ch, grid, false, s));
   return ALOHA_OK;
 }
 

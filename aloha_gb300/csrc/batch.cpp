@@ -49,7 +49,7 @@ int configure(aloha_batch* b) {
   b->total_tiles = prefix.back();
   if (cudaMemcpy(b->d_prefix, prefix.data(), sizeof(int) * prefix.size(), cudaMemcpyHostToDevice) != cudaSuccess)
     return ctx_fail(c, ALOHA_ERR_CUDA, "batch: uploading tile prefix failed");
-  int per_sm = render_blocks_per_sm(b->tile_w, b->tile_h, ctx_n_tf(c));
+  int per_sm = render_blocks_per_sm(b->tile_w, b->tile_h, ctx_n_tf(c), true);
   if (per_sm <= 0) return ctx_fail(c, ALOHA_ERR_CUDA, "batch: occupancy query failed");
   if (b->ctas_per_sm > 0 && b->ctas_per_sm < per_sm) per_sm = b->ctas_per_sm;
   b->grid = ctx_num_sms(c) * per_sm;
@@ -70,7 +70,7 @@ int enqueue(aloha_batch* b, cudaStream_t s) {
   if (cudaMemsetAsync(b->d_work, 0, sizeof(unsigned int), s) != cudaSuccess ||
       cudaMemsetAsync(a.f.counter, 0, sizeof(unsigned long long), s) != cudaSuccess)
     return ctx_fail(c, ALOHA_ERR_CUDA, "batch: memset failed");
-  cudaError_t e = launch_render_warps(a, b->tile_w, b->tile_h, b->grid, s);
+  cudaError_t e = launch_render_warps(a, b->tile_w, b->tile_h, b->grid, true, s);
   if (e != cudaSuccess) return ctx_fail(c, ALOHA_ERR_CUDA, "batch launch: %s", cudaGetErrorString(e));
   ctx_mark_samples(c);
   return ALOHA_OK;

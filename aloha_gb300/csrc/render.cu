@@ -15,10 +15,12 @@ namespace aloha {
 // transfer function is staged): a warp with long rays never holds finished
 // warps of its CTA, and views end without a per-launch tail.  Nothing waits
 // on other warps or CTAs.
-// Six CTAs of 128 threads per SM (80 registers, no spills) keep 24 warps
-// resident to hide the gather latency of the march.
-template <int CW, int CH>
-__global__ void __launch_bounds__(kRenderThreads, 6) render_warps_kernel(BatchArgs b) {
+// MINB CTAs of 128 threads per SM: a single view ends with its slowest
+// chunks, which run faster with more registers per thread (5 CTAs, 96
+// registers); a batch of views is throughput-bound and runs faster with more
+// resident warps (7 CTAs, 72 registers).
+template <int CW, int CH, int MINB>
+__global__ void __launch_bounds__(kRenderThreads, MINB) render_warps_kernel(BatchArgs b) {
   extern __shared__ float4 tf_s[];
   load_tf(tf_s, b.f.tf, b.f.n_tf);
   __syncthreads();
@@ -151,7 +153,7 @@ __global__ void __launch_bounds__(kPlanThreads) split_plan_kernel(SplitArgs s) {
   if (threadIdx.x == kPlanThreads - 1) *s.n_items = at;
 }
 
-__global__ void __launch_bounds__(kRenderThreads, 6) render_split_kernel(SplitArgs s) {
+__global__ void __launch_bounds__(kRenderThreads, kSingleRenderBlocks) render_split_kernel(SplitArgs s) {
   extern __shared__ float4 tf_s[];
   load_tf(tf_s, s.f.tf, s.f.n_tf);
   __syncthreads();
@@ -324,34 +326,37 @@ cudaError_t launch_macrocell_empty(const float2* ranges, int count, const int* p
   return cudaGetLastError();
 }
 
-cudaError_t launch_render_warps(const BatchArgs& b, int chunk_w, int chunk_h, int grid, cudaStream_t s) {
-  const size_t smem = tf_smem(b.f.n_tf);
-  if (chunk_w == 8 && chunk_h == 4)
-    render_warps_kernel<8, 4><<<grid, kRenderThreads, smem, s>>>(b);
-  else if (chunk_w == 8 && chunk_h == 8)
-    render_warps_kernel<8, 8><<<grid, kRenderThreads, smem, s>>>(b);
-  else if (chunk_w == 16 && chunk_h == 8)
-    render_warps_kernel<16, 8><<<grid, kRenderThreads, smem, s>>>(b);
-  else if (chunk_w == 32 && chunk_h == 4)
-    render_warps_kernel<32, 4><<<grid, kRenderThreads, smem, s>>>(b);
-  else
-    return cudaErrorInvalidValue;
+namespace {
+
+// The kernel instance for a chunk shape and launch mode, or null.
+using RenderKernel = void (*)(BatchArgs);
+template <int MINB>
+RenderKernel render_kernel_for(int chunk_w, int chunk_h) {
+  if (chunk_w == 8 && chunk_h == 4) return render_warps_kernel<8, 4, MINB>;
+  if (chunk_w == 8 && chunk_h == 8) return render_warps_kernel<8, 8, MINB>;
+  if (chunk_w == 16 && chunk_h == 8) return render_warps_kernel<16, 8, MINB>;
+  if (chunk_w == 32 && chunk_h == 4) return render_warps_kernel<32, 4, MINB>;
+  return nullptr;
+}
+
+RenderKernel render_kernel(int chunk_w, int chunk_h, bool batch) {
+  return batch ? render_kernel_for<kBatchRenderBlocks>(chunk_w, chunk_h)
+               : render_kernel_for<kSingleRenderBlocks>(chunk_w, chunk_h);
+}
+
+}  // namespace
+
+cudaError_t launch_render_warps(const BatchArgs& b, int chunk_w, int chunk_h, int grid, bool batch, cudaStream_t s) {
+  const RenderKernel k = render_kernel(chunk_w, chunk_h, batch);
+  if (!k) return cudaErrorInvalidValue;
+  k<<<grid, kRenderThreads, tf_smem(b.f.n_tf), s>>>(b);
   return cudaGetLastError();
 }
 
-int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf) {
+int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf, bool batch) {
+  const RenderKernel k = render_kernel(chunk_w, chunk_h, batch);
   int n = 0;
-  const size_t smem = tf_smem(n_tf);
-  cudaError_t e = cudaErrorInvalidValue;
-  if (chunk_w == 8 && chunk_h == 4)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_warps_kernel<8, 4>, kRenderThreads, smem);
-  else if (chunk_w == 8 && chunk_h == 8)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_warps_kernel<8, 8>, kRenderThreads, smem);
-  else if (chunk_w == 16 && chunk_h == 8)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_warps_kernel<16, 8>, kRenderThreads, smem);
-  else if (chunk_w == 32 && chunk_h == 4)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, render_warps_kernel<32, 4>, kRenderThreads, smem);
-  if (e != cudaSuccess) {
+  if (!k || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kRenderThreads, tf_smem(n_tf)) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
