@@ -137,11 +137,11 @@ __device__ __forceinline__ uint32_t train_subtile(const TrainArgs& a, const DevV
     float4 color = make_float4(0.f, 0.f, 0.f, 0.f);
     Checkpoint* ck = a.ckpt + (size_t)pixel * a.ckpt_cap;
     const uint32_t K = a.k, cap = a.ckpt_cap;
-    uint32_t idx = 0;
+    uint32_t left = 0, m = 0;  // samples to the next checkpoint, checkpoints so far
     // checkpoint before every K-th sample, evaluated or skipped
     auto checkpoint = [&](float t, const Walk& w, uint32_t nb, const float4& col) {
-      if (idx % K == 0) {
-        const uint32_t m = idx / K;
+      if (left == 0) {
+        left = K;
         if (m < cap) {
           Checkpoint c;
           c.r = col.x;
@@ -156,8 +156,9 @@ __device__ __forceinline__ uint32_t train_subtile(const TrainArgs& a, const DevV
         } else {
           atomicOr(a.overflow, 1);
         }
+        ++m;
       }
-      ++idx;
+      --left;
     };
     n = walk_samples<true>(a, v, tf_s, ray, pixel, Walk{0, 0.0f, 0u}, 0.f, 0u, false, color, 0xffffffffu,
                            [&](const DevBrick&, float t, const Walk& w, uint32_t nb, float, float, float,
@@ -279,10 +280,10 @@ __device__ __forceinline__ void stencil_backward(const DevBrick& b, const TrainA
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
       const float wyz = wy[j] * wz[l];
-      const float side = dgy * wyg[myc + j] * wz[l] + dgz * wzg[mzc + l] * wy[j];
+      const float side = fmaf(dgy * wyg[myc + j], wz[l], dgz * wzg[mzc + l] * wy[j]);
       float w[3];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) w[k] = wyz * (dgx * wxg[k] + dv * wv[k]) + wv[k] * side;
+      for (int k = 0; k < 3; ++k) w[k] = fmaf(wyz, fmaf(dgx, wxg[k], dv * wv[k]), wv[k] * side);
       scatter3(a, b, org, ix, min(max(cy + j, 0), ny1), min(max(cz + l, 0), nz1), w[0], w[1], w[2]);
     }
   const int ye = min(max(hy ? iy : iy + 2, 0), ny1), ze = min(max(hz ? iz : iz + 2, 0), nz1);
@@ -322,6 +323,8 @@ __device__ __forceinline__ void flush_tf(float* dtf_s, int n, int i, float pend[
   for (int k = 0; k < 8; ++k) pend[k] = 0.f;
 }
 
+constexpr unsigned kBackwardGrab = 256;  // most items a backward warp takes per grab (8 rows of 32)
+
 __global__ void __launch_bounds__(128) backward_kernel(TrainArgs a, int view) {
   extern __shared__ float4 smem[];
   float4* tf_s = smem;                                         // n_tf + 4 entries
@@ -334,66 +337,95 @@ __global__ void __launch_bounds__(128) backward_kernel(TrainArgs a, int view) {
   const unsigned count = min(*a.work_count, a.work_cap);
   const float nf = (float)a.n_tf;
   uint32_t nsamp = 0;
-  for (unsigned item = blockIdx.x * blockDim.x + threadIdx.x; item < count; item += gridDim.x * blockDim.x) {
-    const uint2 wk = a.work[item];
-    const uint32_t pixel = wk.x, m = wk.y;
-    const int x = (int)(pixel % (uint32_t)v.width), y = (int)(pixel / (uint32_t)v.width);
-    const Ray ray = generate_ray(v, x, y);
-    const Checkpoint ck = a.ckpt[(size_t)pixel * a.ckpt_cap + m];
-    const float4 F = a.final_rgba[pixel];
-    const float4 g = a.dl_drgba[pixel];
-    const float gfin = g.w * (1.0f - F.w);
-    float4 color = make_float4(ck.r, ck.g, ck.b, ck.a);
-    const Walk w0{(int)(ck.jd & 0xffffu), ck.tmin, ck.jd >> 16};
-    // transfer-function gradient of consecutive samples with the same lookup
-    // index is summed in registers and added to shared memory once per index
-    int pend_i = INT_MIN;
-    float pend[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    nsamp += walk_samples<false>(
-        a, v, tf_s, ray, pixel, w0, ck.t, ck.nb, true, color, a.k,
-        [&](const DevBrick& b, float, const Walk& wcur, uint32_t, float ux, float uy, float uz, const StencilOut& s,
-            float shade, const float4& c, const float4& col) {
-          float4 nxt = col;  // state after this sample
-          composite_step(nxt, c, shade);
-          const float tn = fmaxf(1.0f - nxt.w, 1e-6f);
-          const float gA = (gfin - (g.x * (F.x - nxt.x) + g.y * (F.y - nxt.y) + g.z * (F.z - nxt.z))) / tn;
-          const float oma = 1.0f - col.w;
-          const float gc = g.x * c.x + g.y * c.y + g.z * c.z;
-          const float kc = oma * c.w * shade;
-          const float dch[4] = {g.x * kc, g.y * kc, g.z * kc, oma * (shade * gc + gA)};
-          const float ds = oma * c.w * gc;
-          // transfer function lookup backward
-          const float xb = s.value * nf - 0.5f;
-          const float fl = floorf(xb);
-          const float wt = xb - fl;
-          const int i0 = (int)fl;
-          const int ic = min(max(i0, -2), a.n_tf);
-          const float4 e0 = tf_s[ic + 2], e1 = tf_s[ic + 3];
-          const float de[4] = {e1.x - e0.x, e1.y - e0.y, e1.z - e0.z, e1.w - e0.w};
-          float dv = 0.f;
-          if (i0 != pend_i) {
-            flush_tf(dtf_s, a.n_tf, pend_i, pend);
-            pend_i = i0;
-          }
-#pragma unroll
-          for (int ch = 0; ch < 4; ++ch) {
-            pend[ch] += (1.f - wt) * dch[ch];
-            pend[4 + ch] += wt * dch[ch];
-            dv += dch[ch] * de[ch] * nf;
-          }
-          // shading backward: s = .1 + .9 |q|, q = (g.d)/|g + 1e-4|
-          const float ex = s.gx + 1e-4f, ey = s.gy + 1e-4f, ez = s.gz + 1e-4f;
-          const float len2 = ex * ex + ey * ey + ez * ez;
-          const float len = sqrtf(len2);
-          const float gd = s.gx * ray.d[0] + s.gy * ray.d[1] + s.gz * ray.d[2];
-          const float q = gd / len;
-          const float kk = ds * 0.9f * (q > 0.f ? 1.f : (q < 0.f ? -1.f : 0.f));
-          const float inv = 1.0f / len, c3 = gd / (len2 * len);
-          stencil_backward(b, a, __ldg(rb + wcur.j), ux, uy, uz, dv, kk * (ray.d[0] * inv - c3 * ex),
-                           kk * (ray.d[1] * inv - c3 * ey), kk * (ray.d[2] * inv - c3 * ez));
-        },
-        [](float, const Walk&, uint32_t, const float4&) {});
-    flush_tf(dtf_s, a.n_tf, pend_i, pend);
+  // Warps take kBackwardGrab consecutive items at a time.  The forward lays
+  // out each of its 8x4 tiles as rows of 32 (segment m of every lane, then
+  // m + 1, ...), so a warp replays consecutive segments of the same rays and
+  // finds the bricks warm in L1 from the previous segment.
+  // The grab shrinks (to one row) when there are too few items to give every
+  // warp several grabs.
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned warps = gridDim.x * (blockDim.x / 32u);
+  const unsigned take = max(32u, min(kBackwardGrab, (count / (warps * 8u)) & ~31u));
+  for (;;) {
+    unsigned grab = 0;
+    if (lane == 0) grab = atomicAdd(a.work_count + 2, take);
+    grab = __shfl_sync(0xffffffffu, grab, 0);
+    if (grab >= count) break;
+    const unsigned end = min(grab + take, count);
+    for (unsigned item = grab + lane; item < end; item += 32u) {
+      const uint2 wk = a.work[item];
+      const uint32_t pixel = wk.x, m = wk.y;
+      const int x = (int)(pixel % (uint32_t)v.width), y = (int)(pixel / (uint32_t)v.width);
+      const Ray ray = generate_ray(v, x, y);
+      const Checkpoint ck = a.ckpt[(size_t)pixel * a.ckpt_cap + m];
+      const float4 F = a.final_rgba[pixel];
+      const float4 g = a.dl_drgba[pixel];
+      const float gfin = g.w * (1.0f - F.w);
+      float4 color = make_float4(ck.r, ck.g, ck.b, ck.a);
+      const Walk w0{(int)(ck.jd & 0xffffu), ck.tmin, ck.jd >> 16};
+      // transfer-function gradient of consecutive samples with the same lookup
+      // index is summed in registers and added to shared memory once per index
+      int pend_i = INT_MIN;
+      float pend[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      nsamp += walk_samples<false>(
+          a, v, tf_s, ray, pixel, w0, ck.t, ck.nb, true, color, a.k,
+          [&](const DevBrick& b, float, const Walk& wcur, uint32_t, float ux, float uy, float uz, const StencilOut& s,
+              float shade, const float4& c, const float4& col) {
+            // Backward-only arithmetic below is free to contract and to use
+            // approximate reciprocals (the gradient tolerance is relative); the
+            // replay that feeds it is the exact forward.
+            float4 nxt = col;  // state after this sample
+            composite_step(nxt, c, shade);
+            const float tn = fmaxf(1.0f - nxt.w, 1e-6f);
+            const float gA = __fdividef(gfin - fmaf(g.x, F.x - nxt.x, fmaf(g.y, F.y - nxt.y, g.z * (F.z - nxt.z))), tn);
+            const float oma = 1.0f - col.w;
+            const float gc = fmaf(g.x, c.x, fmaf(g.y, c.y, g.z * c.z));
+            const float dA = oma * fmaf(shade, gc, gA);  // dL/d(alpha of this sample)
+            // transfer function lookup backward (the lookup of tf_lookup)
+            const float xb = s.value * nf - 0.5f;
+            const float fl = floorf(xb);
+            const float wt = xb - fl;
+            const int i0 = (int)fl;
+            const int ic = min(max(i0, -2), a.n_tf);
+            const float4 e0 = tf_s[ic + 2], e1 = tf_s[ic + 3];
+            if (i0 != pend_i) {
+              flush_tf(dtf_s, a.n_tf, pend_i, pend);
+              pend_i = i0;
+            }
+            if (e0.w == 0.f && e1.w == 0.f) {
+              // Alpha is exactly 0 at this sample: only the two alpha entries of
+              // the lookup receive gradient; the colour entries, the shading and
+              // the density gradients all carry a factor alpha or d(alpha)/dv = 0.
+              pend[3] = fmaf(1.f - wt, dA, pend[3]);
+              pend[7] = fmaf(wt, dA, pend[7]);
+              return;
+            }
+            const float kc = oma * c.w * shade;
+            const float dch[4] = {g.x * kc, g.y * kc, g.z * kc, dA};
+            const float ds = oma * c.w * gc;
+            const float de[4] = {e1.x - e0.x, e1.y - e0.y, e1.z - e0.z, e1.w - e0.w};
+            float dv = 0.f;
+  #pragma unroll
+            for (int ch = 0; ch < 4; ++ch) {
+              pend[ch] = fmaf(1.f - wt, dch[ch], pend[ch]);
+              pend[4 + ch] = fmaf(wt, dch[ch], pend[4 + ch]);
+              dv = fmaf(dch[ch], de[ch], dv);
+            }
+            dv *= nf;
+            // shading backward: s = .1 + .9 |q|, q = (g.d)/|g + 1e-4|
+            const float ex = s.gx + 1e-4f, ey = s.gy + 1e-4f, ez = s.gz + 1e-4f;
+            const float len2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+            const float inv = rsqrtf(len2);
+            const float gd = fmaf(s.gx, ray.d[0], fmaf(s.gy, ray.d[1], s.gz * ray.d[2]));
+            const float kk = ds * 0.9f * (gd > 0.f ? 1.f : (gd < 0.f ? -1.f : 0.f));
+            const float c3 = gd * inv * inv * inv;
+            const float ki = kk * inv, kc3 = kk * c3;
+            stencil_backward(b, a, __ldg(rb + wcur.j), ux, uy, uz, dv, fmaf(ki, ray.d[0], -kc3 * ex),
+                             fmaf(ki, ray.d[1], -kc3 * ey), fmaf(ki, ray.d[2], -kc3 * ez));
+          },
+          [](float, const Walk&, uint32_t, const float4&) {});
+      flush_tf(dtf_s, a.n_tf, pend_i, pend);
+    }
   }
   count_samples(a.counter, nsamp);
   __syncthreads();

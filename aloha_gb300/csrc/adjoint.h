@@ -35,7 +35,8 @@ struct TrainArgs {
   float4* out_rgba;           // [npx] caller's image (forward) or null
   uint2* work;                // [work_cap] (pixel, segment)
   unsigned work_cap;
-  unsigned* work_count;        // [0] segments appended, [1] chunk counter of the forward
+  unsigned* work_count;        // [0] segments appended, [1] chunk counter of the forward,
+                               // [2] item counter of the backward
   int* overflow;              // set when a pixel needs more checkpoints than ckpt_cap
   const float4* dl_drgba;     // [npx] backward input
   float* dtf;                 // [n_tf*4] accumulated

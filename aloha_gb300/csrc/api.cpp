@@ -1097,7 +1097,7 @@ int aloha_forward(aloha_ctx* c, int view, float* rgba, int checkpoint_every, voi
     CUDA_TRY(c, cudaMalloc(&t.ckpt, npx * cap * sizeof(Checkpoint)));
     CUDA_TRY(c, cudaMalloc(&t.work, npx * cap * sizeof(uint2)));
     CUDA_TRY(c, cudaMalloc(&t.final_rgba, npx * sizeof(float4)));
-    CUDA_TRY(c, cudaMalloc(&t.work_count, 2 * sizeof(unsigned)));
+    CUDA_TRY(c, cudaMalloc(&t.work_count, 4 * sizeof(unsigned)));
     CUDA_TRY(c, cudaMalloc(&t.overflow, sizeof(int)));
     t.npx = npx;
     t.cap = cap;
@@ -1107,7 +1107,7 @@ int aloha_forward(aloha_ctx* c, int view, float* rgba, int checkpoint_every, voi
   TrainArgs a = train_args(c, t);
   const bool host = !is_device_pointer(rgba);
   a.out_rgba = host ? nullptr : reinterpret_cast<float4*>(rgba);
-  CUDA_TRY(c, cudaMemsetAsync(t.work_count, 0, 2 * sizeof(unsigned), s));
+  CUDA_TRY(c, cudaMemsetAsync(t.work_count, 0, 4 * sizeof(unsigned), s));
   CUDA_TRY(c, cudaMemsetAsync(t.overflow, 0, sizeof(int), s));
   CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
   const int per_sm = forward_train_blocks_per_sm(c->n_tf);
@@ -1172,6 +1172,7 @@ int aloha_backward(aloha_ctx* c, int view, const float* dl_drgba, float* dl_dtf,
   const int per_sm = backward_blocks_per_sm(c->n_tf);
   if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "backward occupancy query failed");
   CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
+  CUDA_TRY(c, cudaMemsetAsync(a.work_count + 2, 0, sizeof(unsigned), s));  // the backward's grab counter
   CUDA_TRY(c, launch_backward(a, view, c->num_sms * per_sm, s));
   CUDA_TRY(c, launch_fold_quads(a.dgrid4, grid_out, grid_dims, s));
   c->samples_valid = true;

@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-case", choices=["small", "volume"], default="small",
+                    help="with --only-adjoint: the 128^3 single-brick case, or the bench volume (--n, --size) "
+                         "in 8 bricks as one rank over 2 cameras")
     ap.add_argument("--only-adjoint", action="store_true",
                     help="run only the 128^3, 16 x 256^2 forward + adjoint configuration and print its timings")
     ap.add_argument("--profile", action="store_true", help="short run for ncu (no baselines, no clocks)")
@@ -267,10 +270,15 @@ def main():
     dev = torch.device("cuda", local)
     if args.only_adjoint:
         from aloha_gb300 import scenes as S
-        v4 = S.blob_field((128, 128, 128), 16, (4.0, 12.0), seed=4001, device=dev)
-        c4 = S.orbit_cameras((128, 128, 128), 16, 256, 256, seed=4002)
-        res = adjoint_section("128^3 single brick, 16 x 256^2", v4, S.single_brick((128, 128, 128)), c4, 256, 256,
-                              32, torch.cuda.current_stream(), dev)
+        if args.adjoint_case == "volume":
+            vol, descs, _, _, cams = build_scene(args, dev)
+            res = adjoint_section(f"{args.n}^3 @{args.size}^2, 8 bricks as 1 rank", vol, descs, cams[:2], args.size,
+                                  args.size, 32, torch.cuda.current_stream(), dev)
+        else:
+            v4 = S.blob_field((128, 128, 128), 16, (4.0, 12.0), seed=4001, device=dev)
+            c4 = S.orbit_cameras((128, 128, 128), 16, 256, 256, seed=4002)
+            res = adjoint_section("128^3 single brick, 16 x 256^2", v4, S.single_brick((128, 128, 128)), c4, 256,
+                                  256, 32, torch.cuda.current_stream(), dev)
         print(json.dumps(res), flush=True)
         return
 
