@@ -71,7 +71,9 @@ class _Render(torch.autograd.Function):
     def backward(ctx, grad):
         r: DifferentiableRenderer = ctx.renderer
         grad = grad.contiguous().float()
-        dtf = torch.zeros(ctx.tf_shape, dtype=torch.float32, device=grad.device)
+        # without a transfer-function gradient the backward skips empty space
+        dtf = torch.zeros(ctx.tf_shape, dtype=torch.float32, device=grad.device) \
+            if ctx.needs_input_grad[0] else None
         dden = torch.zeros(ctx.density_shape, dtype=torch.float32, device=grad.device)
         stream = torch.cuda.current_stream()
         nz, ny, nx = ctx.density_shape

@@ -325,12 +325,18 @@ __device__ __forceinline__ void flush_tf(float* dtf_s, int n, int i, float pend[
 
 constexpr unsigned kBackwardGrab = 256;  // most items a backward warp takes per grab (8 rows of 32)
 
-__global__ void __launch_bounds__(128) backward_kernel(TrainArgs a, int view) {
+// WITH_TF: also the transfer-function gradient.  Without it (density only)
+// the replay skips empty macrocells like the forward: a sample there has
+// transfer-function alpha 0 at both lookup entries, so its density and
+// shading gradients vanish and only the alpha entries would receive any.
+template <bool WITH_TF>
+__global__ void __launch_bounds__(128, 5) backward_kernel(TrainArgs a, int view) {
   extern __shared__ float4 smem[];
   float4* tf_s = smem;                                         // n_tf + 4 entries
-  float* dtf_s = reinterpret_cast<float*>(smem + a.n_tf + 4);  // n_tf * 4
+  float* dtf_s = reinterpret_cast<float*>(smem + a.n_tf + 4);  // n_tf * 4 (WITH_TF)
   load_tf(tf_s, a.tf, a.n_tf);
-  for (int i = threadIdx.x; i < a.n_tf * 4; i += blockDim.x) dtf_s[i] = 0.f;
+  if (WITH_TF)
+    for (int i = threadIdx.x; i < a.n_tf * 4; i += blockDim.x) dtf_s[i] = 0.f;
   __syncthreads();
   const DevView v = a.views[view];
   const int* __restrict__ rb = rank_bricks(a, v);
@@ -367,7 +373,7 @@ __global__ void __launch_bounds__(128) backward_kernel(TrainArgs a, int view) {
       // index is summed in registers and added to shared memory once per index
       int pend_i = INT_MIN;
       float pend[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      nsamp += walk_samples<false>(
+      nsamp += walk_samples<!WITH_TF>(
           a, v, tf_s, ray, pixel, w0, ck.t, ck.nb, true, color, a.k,
           [&](const DevBrick& b, float, const Walk& wcur, uint32_t, float ux, float uy, float uz, const StencilOut& s,
               float shade, const float4& c, const float4& col) {
@@ -388,7 +394,7 @@ __global__ void __launch_bounds__(128) backward_kernel(TrainArgs a, int view) {
             const int i0 = (int)fl;
             const int ic = min(max(i0, -2), a.n_tf);
             const float4 e0 = tf_s[ic + 2], e1 = tf_s[ic + 3];
-            if (i0 != pend_i) {
+            if (WITH_TF && i0 != pend_i) {
               flush_tf(dtf_s, a.n_tf, pend_i, pend);
               pend_i = i0;
             }
@@ -396,8 +402,10 @@ __global__ void __launch_bounds__(128) backward_kernel(TrainArgs a, int view) {
               // Alpha is exactly 0 at this sample: only the two alpha entries of
               // the lookup receive gradient; the colour entries, the shading and
               // the density gradients all carry a factor alpha or d(alpha)/dv = 0.
-              pend[3] = fmaf(1.f - wt, dA, pend[3]);
-              pend[7] = fmaf(wt, dA, pend[7]);
+              if (WITH_TF) {
+                pend[3] = fmaf(1.f - wt, dA, pend[3]);
+                pend[7] = fmaf(wt, dA, pend[7]);
+              }
               return;
             }
             const float kc = oma * c.w * shade;
@@ -407,8 +415,10 @@ __global__ void __launch_bounds__(128) backward_kernel(TrainArgs a, int view) {
             float dv = 0.f;
   #pragma unroll
             for (int ch = 0; ch < 4; ++ch) {
-              pend[ch] = fmaf(1.f - wt, dch[ch], pend[ch]);
-              pend[4 + ch] = fmaf(wt, dch[ch], pend[4 + ch]);
+              if (WITH_TF) {
+                pend[ch] = fmaf(1.f - wt, dch[ch], pend[ch]);
+                pend[4 + ch] = fmaf(wt, dch[ch], pend[4 + ch]);
+              }
               dv = fmaf(dch[ch], de[ch], dv);
             }
             dv *= nf;
@@ -424,15 +434,19 @@ __global__ void __launch_bounds__(128) backward_kernel(TrainArgs a, int view) {
                              fmaf(ki, ray.d[1], -kc3 * ey), fmaf(ki, ray.d[2], -kc3 * ez));
           },
           [](float, const Walk&, uint32_t, const float4&) {});
-      flush_tf(dtf_s, a.n_tf, pend_i, pend);
+      if (WITH_TF) flush_tf(dtf_s, a.n_tf, pend_i, pend);
     }
   }
   count_samples(a.counter, nsamp);
-  __syncthreads();
-  for (int i = threadIdx.x; i < a.n_tf * 4; i += blockDim.x) red_add(a.dtf + i, dtf_s[i]);
+  if (WITH_TF) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < a.n_tf * 4; i += blockDim.x) red_add(a.dtf + i, dtf_s[i]);
+  }
 }
 
-size_t backward_smem(int n_tf) { return (size_t)(n_tf + 4) * sizeof(float4) + (size_t)n_tf * 4 * sizeof(float); }
+size_t backward_smem(int n_tf, bool with_tf) {
+  return (size_t)(n_tf + 4) * sizeof(float4) + (with_tf ? (size_t)n_tf * 4 * sizeof(float) : 0);
+}
 
 }  // namespace
 
@@ -456,12 +470,14 @@ int forward_train_blocks_per_sm(int n_tf) {
 }
 
 cudaError_t launch_backward(const TrainArgs& a, int view, int grid, cudaStream_t s) {
-  const size_t smem = backward_smem(a.n_tf);
+  const bool with_tf = a.dtf != nullptr;
+  const size_t smem = backward_smem(a.n_tf, with_tf);
+  void (*k)(TrainArgs, int) = with_tf ? backward_kernel<true> : backward_kernel<false>;
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  backward_kernel<<<grid, 128, smem, s>>>(a, view);
+  k<<<grid, 128, smem, s>>>(a, view);
   return cudaGetLastError();
 }
 
@@ -475,14 +491,16 @@ cudaError_t launch_fold_quads(const float4* quads, float* out, const int dims[3]
 }
 
 int backward_blocks_per_sm(int n_tf) {
-  const size_t smem = backward_smem(n_tf);
+  // the instance with the transfer-function gradient needs more shared memory
+  const size_t smem = backward_smem(n_tf, true);
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+      cudaFuncSetAttribute(backward_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, backward_kernel, 128, smem) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, backward_kernel<true>, 128, smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }

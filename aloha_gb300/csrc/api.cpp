@@ -1121,7 +1121,7 @@ int aloha_forward(aloha_ctx* c, int view, float* rgba, int checkpoint_every, voi
 
 int aloha_backward(aloha_ctx* c, int view, const float* dl_drgba, float* dl_dtf, float* dl_ddensity,
                    const int* grid_lo, const int* grid_dims, void* stream) {
-  if (!c || !dl_drgba || !dl_dtf || !dl_ddensity || !grid_lo || !grid_dims) return ALOHA_ERR_NULL_POINTER;
+  if (!c || !dl_drgba || !dl_ddensity || !grid_lo || !grid_dims) return ALOHA_ERR_NULL_POINTER;
   if (view < 0 || view >= (int)c->views.size()) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "view %d", view);
   int rc = check_trainable(c);
   if (rc) return rc;
@@ -1147,7 +1147,7 @@ int aloha_backward(aloha_ctx* c, int view, const float* dl_drgba, float* dl_dtf,
   CUDA_TRY(c, cudaStreamSynchronize(s));
   if (overflow) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "a ray needed more checkpoints than reserved");
   const size_t npx = t.npx, tf_bytes = (size_t)c->n_tf * 4 * sizeof(float), g_bytes = grid_elems * sizeof(float);
-  const bool h_dl = !is_device_pointer(dl_drgba), h_tf = !is_device_pointer(dl_dtf),
+  const bool h_dl = !is_device_pointer(dl_drgba), h_tf = dl_dtf && !is_device_pointer(dl_dtf),
              h_grid = !is_device_pointer(dl_ddensity);
   // device staging for host arguments, in one block: dL/dRGBA, dL/dtf, dL/ddensity, origins
   const size_t off_tf = h_dl ? npx * sizeof(float4) : 0;

@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--adjoint-case", choices=["small", "volume"], default="small",
                     help="with --only-adjoint: the 128^3 single-brick case, or the bench volume (--n, --size) "
                          "in 8 bricks as one rank over 2 cameras")
+    ap.add_argument("--adjoint-k", type=int, default=32, help="checkpoint every K samples in the adjoint sections")
     ap.add_argument("--only-adjoint", action="store_true",
                     help="run only the 128^3, 16 x 256^2 forward + adjoint configuration and print its timings")
     ap.add_argument("--profile", action="store_true", help="short run for ncu (no baselines, no clocks)")
@@ -273,12 +274,12 @@ def main():
         if args.adjoint_case == "volume":
             vol, descs, _, _, cams = build_scene(args, dev)
             res = adjoint_section(f"{args.n}^3 @{args.size}^2, 8 bricks as 1 rank", vol, descs, cams[:2], args.size,
-                                  args.size, 32, torch.cuda.current_stream(), dev)
+                                  args.size, args.adjoint_k, torch.cuda.current_stream(), dev)
         else:
             v4 = S.blob_field((128, 128, 128), 16, (4.0, 12.0), seed=4001, device=dev)
             c4 = S.orbit_cameras((128, 128, 128), 16, 256, 256, seed=4002)
             res = adjoint_section("128^3 single brick, 16 x 256^2", v4, S.single_brick((128, 128, 128)), c4, 256,
-                                  256, 32, torch.cuda.current_stream(), dev)
+                                  256, args.adjoint_k, torch.cuda.current_stream(), dev)
         print(json.dumps(res), flush=True)
         return
 
@@ -413,13 +414,13 @@ def main():
         if not args.no_adjoint and rank == 0:
             from aloha_gb300 import scenes as S
             # the headline volume and image as one virtual rank
-            adj = [adjoint_section("512^3 @1024^2, 8 bricks as 1 rank", vol, descs, cams[:4], W, H, 32, stream,
-                                   dev)]
-            # the differentiable configuration: 128^3 single brick, 16 views at 256^2, K = 32
+            adj = [adjoint_section("512^3 @1024^2, 8 bricks as 1 rank", vol, descs, cams[:4], W, H, args.adjoint_k,
+                                   stream, dev)]
+            # the differentiable configuration: 128^3 single brick, 16 views at 256^2
             v4 = S.blob_field((128, 128, 128), 16, (4.0, 12.0), seed=4001, device=dev)
             c4 = S.orbit_cameras((128, 128, 128), 16, 256, 256, seed=4002)
             adj.append(adjoint_section("128^3 single brick, 16 x 256^2", v4, S.single_brick((128, 128, 128)), c4,
-                                       256, 256, 32, stream, dev))
+                                       256, 256, args.adjoint_k, stream, dev))
             result["adjoint"] = adj
 
         if not args.no_cpu_baseline and rank == 0:
@@ -468,9 +469,9 @@ def adjoint_section(name, vol, descs, cams, W, H, k, stream, dev):
         for v in range(nv):
             ctx.forward(v, img[v], k, stream)
 
-    def bwd(grad):
+    def bwd(grad, with_tf=True):
         for v in range(nv):
-            ctx.backward(v, grad[v], dtf, dden, (0, 0, 0), (n, n, n), stream)
+            ctx.backward(v, grad[v], dtf if with_tf else None, dden, (0, 0, 0), (n, n, n), stream)
 
     fwd()
     grad = (2.0 * (img - target)).contiguous()
@@ -493,10 +494,23 @@ def adjoint_section(name, vol, descs, cams, W, H, k, stream, dev):
         torch.cuda.synchronize()
         fwd_ms += e[0].elapsed_time(e[1]) / reps
         bwd_ms += e[1].elapsed_time(e[2]) / reps
+    # density gradient only (the backward skips empty space)
+    den_ms = 0.0
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        e[0].record(stream)
+        fwd()
+        e[1].record(stream)
+        bwd(grad, with_tf=False)
+        e[2].record(stream)
+        torch.cuda.synchronize()
+        den_ms += e[1].elapsed_time(e[2]) / reps
     ctx.close()
     return {"config": name, "views": nv, "image": [W, H], "checkpoint_every": k,
             "fwd_ms_per_view": fwd_ms / nv, "adjoint_ms_per_view": bwd_ms / nv,
             "fwd_plus_adjoint_over_fwd": (fwd_ms + bwd_ms) / fwd_ms,
+            "adjoint_density_only_ms_per_view": den_ms / nv,
+            "fwd_plus_density_adjoint_over_fwd": (fwd_ms + den_ms) / fwd_ms,
             "fwd_gsamples_per_s": samples / (fwd_ms * 1e-3) / 1e9,
             "fwd_plus_adjoint_gsamples_per_s": samples / ((fwd_ms + bwd_ms) * 1e-3) / 1e9}
 

@@ -233,7 +233,10 @@ int aloha_forward(aloha_ctx* ctx, int view, float* rgba, int checkpoint_every, v
  * ([height][width][4] float).  Accumulates (+=) into dl_dtf ([n_tf][4]) and
  * into dl_ddensity, a float grid [dims z][dims y][dims x] whose voxel (0,0,0)
  * is grid_lo; every brick's voxel range must lie inside it.  Ghost voxels and
- * clamped edge taps add into the voxel they copy.  Host or device buffers. */
+ * clamped edge taps add into the voxel they copy.  Host or device buffers.
+ * dl_dtf may be NULL: only the density gradient is computed, and the replay
+ * then skips empty macrocells (their samples have transfer-function alpha 0,
+ * so they contribute to the alpha entries of dl_dtf only). */
 int aloha_backward(aloha_ctx* ctx, int view, const float* dl_drgba, float* dl_dtf, float* dl_ddensity,
                    const int* grid_lo, const int* grid_dims, void* stream);
 

@@ -79,6 +79,34 @@ def test_backward_matches_fp64_oracle(gpu_ctx_factory, oracle, bricks, k):
     assert np.count_nonzero(dden) > 1000
 
 
+@pytest.mark.parametrize("bricks", [1, 8])
+def test_density_only_backward(gpu_ctx_factory, oracle, bricks):
+    """Without a transfer-function gradient the backward skips empty
+    macrocells; its density gradient must still match the FP64 oracle and the
+    full backward's (up to the order of the atomic adds)."""
+    n = 48
+    vol, descs, vox = density_scene(n, seed=9, bricks=bricks)
+    tf = S.ramp_tf()
+    W, H = 80, 72
+    ctx = setup(gpu_ctx_factory, descs, vox, tf)
+    rng = np.random.default_rng(31 + bricks)
+    full_tf = np.zeros((tf.shape[0], 4), np.float32)
+    full_den = np.zeros((n, n, n), np.float32)
+    only_den = np.zeros((n, n, n), np.float32)
+    ref_den = np.zeros((n, n, n))
+    for v, cam in enumerate(T.cameras((n, n, n), 2, W, H, seed=17)):
+        ctx.set_camera(v, *cam)
+        ctx.resize(v, W, H)
+        ctx.forward(v, np.zeros((H, W, 4), np.float32), 32)
+        dl = rng.uniform(-1, 1, (H, W, 4)).astype(np.float32)
+        ctx.backward(v, dl, full_tf, full_den, (0, 0, 0), (n, n, n))
+        ctx.backward(v, dl, None, only_den, (0, 0, 0), (n, n, n))
+        ref_den += oracle.adjoint(descs, vox, tf, oracle.make_camera(*cam), W, H, dl, (0, 0, 0), (n, n, n))["ddensity"]
+    assert np.count_nonzero(only_den) > 1000
+    assert rel_err(only_den, ref_den) < 1e-3
+    np.testing.assert_allclose(only_den, full_den, rtol=1e-4, atol=1e-6 * float(np.abs(full_den).max()))
+
+
 def _loss(ctx, views, W, H, weights):
     total = 0.0
     for v in views:
