@@ -357,13 +357,17 @@ bool rank_split_possible(const aloha_ctx* c, const FrameArgs& f, const ViewState
          ring_slots(v.width, v.height, 8, 4) < (1 << 25);
 }
 
-// Automatic mode keeps the pixel split: on a 512^3 volume in 8 bricks at
-// 1024^2 it measured faster (the longest chunks spend most of their samples
-// inside one brick, so the rank split adds ticket and plane traffic without
-// shortening them).
+// Automatic mode: the pixel split for few ranks, the rank split for many.
+// 8 bricks of a 512^3 volume at 1024^2: pixels 0.99 ms, ranks 1.15 ms (the
+// longest chunks spend most of their samples inside one brick).  64 bricks of
+// a 1024^3 volume at 2048^2: pixels 7.08 ms, ranks 6.58 ms (each pixel walks
+// 64 ranks in the pixel split; most chunks are covered by few of them).
+constexpr int kAutoRankSplitRanks = 32;
+
 bool use_rank_split(const aloha_ctx* c, const FrameArgs& f, const ViewState& v) {
-  return c->split_mode == ALOHA_SPLIT_RANKS && rank_split_possible(c, f, v) &&
-         split_scratch_bytes(c, v) <= kSplitScratchCap;
+  if (c->split_mode == ALOHA_SPLIT_PIXELS || !rank_split_possible(c, f, v)) return false;
+  if (c->split_mode == ALOHA_SPLIT_AUTO && c->n_ranks < kAutoRankSplitRanks) return false;
+  return split_scratch_bytes(c, v) <= kSplitScratchCap;
 }
 
 // Rank-split launch of a single view (mask, plan and render kernels).

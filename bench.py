@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the 1024^3 / 64-brick / 2048^2 section (about 110 GB of device memory)")
     ap.add_argument("--adjoint-case", choices=["small", "volume"], default="small",
                     help="with --only-adjoint: the 128^3 single-brick case, or the bench volume (--n, --size) "
                          "in 8 bricks as one rank over 2 cameras")
@@ -431,6 +433,10 @@ def main():
             result["cpu_baseline"] = {"value": s / sec / 1e9, "unit": "Gsamples/s", "cores": thr, "kind": "port",
                                       "sample": f"{rows} rows (16-row bands, 8 per view) of {nv} view(s) at {W} px, "
                                                 f"{s} samples in {sec:.1f} s"}
+        if not args.no_large and rank == 0:
+            ctx.close()
+            torch.cuda.empty_cache()
+            result["large"] = large_section(dev)
     if rank == 0:
         print(json.dumps(result), flush=True)
     ctx.close()
@@ -550,6 +556,89 @@ def batched_section(ctx, cams, mine, W, H, args, stream, dev, samples_of):
     b.close()
     return {"views": nv, "tile": [tw, th], "ms_batch": ms_graph, "ms_plain_launches": ms_plain,
             "speedup_vs_plain": ms_plain / ms_graph, "gsamples_per_s": samples / (ms_graph * 1e-3) / 1e9}
+
+
+def large_section(dev, n=1024, size=2048, views=8, k=64):
+    """The large configuration: 1024^3 fp32 blobs in 4x4x4 bricks, 8 views at
+    2048^2.  Render with 64 virtual ranks (both work divisions, plain and
+    batched), then forward plus adjoint (TF and density) over the 8 views as
+    one virtual rank with a checkpoint every 64 samples."""
+    import torch
+
+    from aloha_gb300 import abi
+    from aloha_gb300 import scenes as S
+    from aloha_gb300 import volfile as V
+    dims = (n, n, n)
+    stream = torch.cuda.current_stream()
+    vol = S.blob_field(dims, 64, (n / 16.0, n / 6.4), seed=5001, device=dev)
+    descs = V.chopsuey_split(dims, 64)
+    ctx = abi.Context(dev.index or 0)
+    ctx.set_bricks(descs, [V.brick_voxels(vol, d) for d in descs])
+    del vol
+    torch.cuda.empty_cache()
+    ctx.set_transfer_function(S.ramp_tf())
+    ctx.set_ranks(len(descs))
+    ctx.set_params()
+    cams = S.orbit_cameras(dims, views, size, size, seed=5004)
+    for v, cam in enumerate(cams):
+        ctx.set_camera(v, *cam)
+        ctx.resize(v, size, size)
+    fbs = [torch.zeros((size, size), dtype=torch.int32, device=dev) for _ in cams]
+
+    def timed(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    samples = 0
+    for v in range(views):
+        ctx.render(v, fbs[v], stream)
+        samples += ctx.stats().samples
+    out = {"config": f"{n}^3 fp32 in {len(descs)} bricks ({len(descs)} virtual ranks), {views} views at {size}^2",
+           "samples_per_view": samples / views}
+    for name, split in (("pixels", abi.SPLIT_PIXELS), ("ranks", abi.SPLIT_RANKS)):
+        ctx.set_render_split(split)
+        ms = timed(lambda: [ctx.render(v, fbs[v], stream) for v in range(views)]) / views
+        out[f"render_{name}_ms_per_view"] = ms
+        out[f"render_{name}_gsamples_per_s"] = samples / views / (ms * 1e-3) / 1e9
+    ctx.set_render_split(abi.SPLIT_AUTO)
+    b = ctx.batch(list(range(views)), fbs)
+    b.autotune(stream, reps=1)
+    ms = timed(lambda: b.launch_graph(stream)) / views
+    b.close()
+    out["batched_ms_per_view"] = ms
+    out["batched_gsamples_per_s"] = samples / views / (ms * 1e-3) / 1e9
+    # forward + adjoint as one virtual rank
+    ctx.set_ranks(1)
+    img = torch.empty((views, size, size, 4), dtype=torch.float32, device=dev)
+    dtf = torch.zeros((256, 4), dtype=torch.float32, device=dev)
+    dden = torch.zeros(dims, dtype=torch.float32, device=dev)
+    g = torch.Generator(device=dev).manual_seed(5005)
+    dl = (torch.rand((size, size, 4), generator=g, device=dev) * 2.0 - 1.0).contiguous()
+
+    def fwd():
+        for v in range(views):
+            ctx.forward(v, img[v], k, stream)
+
+    def bwd(with_tf=True):
+        for v in range(views):
+            ctx.backward(v, dl, dtf if with_tf else None, dden, (0, 0, 0), dims, stream)
+
+    fwd_ms = timed(fwd) / views
+    bwd_ms = timed(bwd) / views
+    den_ms = timed(lambda: bwd(False)) / views
+    ctx.close()
+    out.update({"checkpoint_every": k, "fwd_ms_per_view": fwd_ms, "adjoint_ms_per_view": bwd_ms,
+                "fwd_plus_adjoint_over_fwd": (fwd_ms + bwd_ms) / fwd_ms,
+                "adjoint_density_only_ms_per_view": den_ms,
+                "fwd_plus_density_adjoint_over_fwd": (fwd_ms + den_ms) / fwd_ms})
+    return out
 
 
 if __name__ == "__main__":

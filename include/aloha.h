@@ -150,8 +150,9 @@ int aloha_set_render_tile(aloha_ctx* ctx, int tile_w, int tile_h);
  * it.  Both give bit-identical frames.  The rank split needs 2..64 virtual
  * ranks and at most 16 GiB of scratch (else ALOHA_ERR_UNSUPPORTED);
  * aloha_render_partials and a single rank always use the pixel split.
- * ALOHA_SPLIT_AUTO (the default) is the pixel split.  No reference
- * counterpart (each reference rank is its own process). */
+ * ALOHA_SPLIT_AUTO (the default) takes the rank split from 32 virtual ranks
+ * up (when it applies) and the pixel split below.  No reference counterpart
+ * (each reference rank is its own process). */
 int aloha_set_render_split(aloha_ctx* ctx, int mode);
 
 /* Render one view into an RGBA8 frame buffer of width*height uint32
