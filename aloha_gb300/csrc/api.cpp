@@ -347,7 +347,7 @@ constexpr size_t kSplitScratchCap = size_t(16) << 30;  // rank split scratch lim
 // item list, tickets.
 size_t split_scratch_bytes(const aloha_ctx* c, const ViewState& v) {
   const size_t slots = (size_t)ring_slots(v.width, v.height, 8, 4);
-  return (size_t)c->n_ranks * v.width * v.height * sizeof(float4) + slots * (8 + 4 + 4 * (size_t)c->n_ranks);
+  return (size_t)c->n_ranks * v.width * v.height * sizeof(float4) + slots * (8 + 4 + 4 + 4 * (size_t)c->n_ranks);
 }
 
 // The rank split serves aloha_render (a frame buffer, no rank planes wanted)
@@ -380,8 +380,9 @@ int launch_split(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   a.n_slots = ring_slots(v.width, v.height, 8, 4);
   CUDA_TRY(c, c->split_images.ensure((size_t)R * v.width * v.height * sizeof(float4)));
   a.f.rank_images = static_cast<float4*>(c->split_images.ptr);
-  CUDA_TRY(c, c->split_masks.ensure((size_t)a.n_slots * sizeof(unsigned long long)));
+  CUDA_TRY(c, c->split_masks.ensure((size_t)a.n_slots * (sizeof(unsigned long long) + sizeof(uint32_t))));
   a.masks = static_cast<unsigned long long*>(c->split_masks.ptr);
+  a.offsets = reinterpret_cast<uint32_t*>(a.masks + a.n_slots);
   CUDA_TRY(c, c->split_items.ensure((size_t)a.n_slots * R * sizeof(uint32_t) + 16));
   a.items = static_cast<uint32_t*>(c->split_items.ptr);
   a.n_items = reinterpret_cast<uint32_t*>(static_cast<char*>(c->split_items.ptr) + (size_t)a.n_slots * R * 4);

@@ -95,6 +95,7 @@ struct SplitArgs {
   int view;
   int n_slots;                     // ring slots of 8x4 chunks (< 2^25)
   unsigned long long* masks;       // [n_slots] covering ranks per slot
+  uint32_t* offsets;               // [n_slots] first item of each slot
   uint32_t* items;                 // [n_slots * max(1, n_ranks)] slot << 7 | rank position
   uint32_t* n_items;               // items listed (written by the plan kernel)
   unsigned int* chunk_done;        // [n_slots] tickets, zero between launches

@@ -70,9 +70,9 @@ __global__ void __launch_bounds__(kRenderThreads, MINB) render_warps_kernel(Batc
 // split_mask_kernel marks, per chunk slot, the ranks whose screen rectangle
 // covers the chunk (bit k = k-th rank in visibility order); no pixel ray of
 // an unmarked rank can enter its bricks, so its image is the output stage of
-// an empty march.  split_plan_kernel lists the work items in slot order
-// (centre-out): one per marked rank, or one compositing-only item for a chunk
-// no rank covers.  render_split_kernel marches each item's rank into its
+// an empty march.  split_scan_kernel and split_emit_kernel list the work items
+// in slot order (centre-out): one per marked rank, or one compositing-only
+// item for a chunk no rank covers.  render_split_kernel marches each item's rank into its
 // image plane; the warp that completes a chunk's last marked rank (a ticket
 // per chunk, taken after a fence) blends the chunk front to back, evaluating
 // the unmarked ranks' images in place, and resets the ticket for the next
@@ -82,6 +82,8 @@ __device__ __forceinline__ bool rect_covers(const int* __restrict__ q, int cx, i
   return cx >= __ldg(q) && cy >= __ldg(q + 1) && cx <= __ldg(q + 2) && cy <= __ldg(q + 3);
 }
 
+// Per slot: the mask of covering ranks and the number of items it lists
+// (one per covering rank, one for a covered-by-none chunk, 0 off the grid).
 __global__ void split_mask_kernel(SplitArgs s) {
   const DevView& v = s.f.views[s.view];
   const int W = v.width, H = v.height, R = v.n_ranks;
@@ -91,30 +93,27 @@ __global__ void split_mask_kernel(SplitArgs s) {
   for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < s.n_slots; slot += gridDim.x * blockDim.x) {
     int cx, cy;
     unsigned long long m = 0ull;
-    if (ring_chunk(slot, cxn, cyn, cx, cy))
+    uint32_t items = 0;
+    if (ring_chunk(slot, cxn, cyn, cx, cy)) {
       for (int k = 0; k < R; ++k)
         if (rect_covers(rects + 4 * __ldg(order + k), cx, cy)) m |= 1ull << k;
+      items = m ? (uint32_t)__popcll(m) : 1u;
+    }
     s.masks[slot] = m;
+    s.offsets[slot] = items;
   }
 }
 
 constexpr int kPlanThreads = 1024;
 
-__device__ __forceinline__ uint32_t slot_items(int slot, int cxn, int cyn, unsigned long long m) {
-  int cx, cy;
-  if (!ring_chunk(slot, cxn, cyn, cx, cy)) return 0u;
-  return m ? (uint32_t)__popcll(m) : 1u;
-}
-
-__global__ void __launch_bounds__(kPlanThreads) split_plan_kernel(SplitArgs s) {
+// Exclusive scan of the per-slot item counts in place (one CTA; each thread
+// scans a contiguous range) and the item total.
+__global__ void __launch_bounds__(kPlanThreads) split_scan_kernel(SplitArgs s) {
   __shared__ uint32_t warp_sum[kPlanThreads / 32];
-  const DevView& v = s.f.views[s.view];
-  const int cxn = (v.width + 7) / 8, cyn = (v.height + 3) / 4;
   const int per = (s.n_slots + kPlanThreads - 1) / kPlanThreads;
   const int lo = min(s.n_slots, (int)threadIdx.x * per), hi = min(s.n_slots, lo + per);
   uint32_t count = 0;
-  for (int slot = lo; slot < hi; ++slot) count += slot_items(slot, cxn, cyn, s.masks[slot]);
-  // exclusive block scan of the per-thread counts
+  for (int i = lo; i < hi; ++i) count += s.offsets[i];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   uint32_t incl = count;
 #pragma unroll
@@ -135,13 +134,27 @@ __global__ void __launch_bounds__(kPlanThreads) split_plan_kernel(SplitArgs s) {
   }
   __syncthreads();
   uint32_t at = incl - count + (wid > 0 ? warp_sum[wid - 1] : 0u);
-  for (int slot = lo; slot < hi; ++slot) {
+  for (int i = lo; i < hi; ++i) {
+    const uint32_t c = s.offsets[i];
+    s.offsets[i] = at;
+    at += c;
+  }
+  if (threadIdx.x == kPlanThreads - 1) *s.n_items = at;
+}
+
+// Writes each slot's items at its offset: slot << 7 | rank position, or the
+// compositing-only item of a chunk no rank covers.
+__global__ void split_emit_kernel(SplitArgs s) {
+  const DevView& v = s.f.views[s.view];
+  const int cxn = (v.width + 7) / 8, cyn = (v.height + 3) / 4;
+  for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < s.n_slots; slot += gridDim.x * blockDim.x) {
     int cx, cy;
     if (!ring_chunk(slot, cxn, cyn, cx, cy)) continue;
+    uint32_t at = s.offsets[slot];
     unsigned long long m = s.masks[slot];
     const uint32_t base = (uint32_t)slot << 7;
     if (!m) {
-      s.items[at++] = base | kSplitBackground;
+      s.items[at] = base | kSplitBackground;
       continue;
     }
     while (m) {
@@ -150,7 +163,6 @@ __global__ void __launch_bounds__(kPlanThreads) split_plan_kernel(SplitArgs s) {
       s.items[at++] = base | (uint32_t)k;
     }
   }
-  if (threadIdx.x == kPlanThreads - 1) *s.n_items = at;
 }
 
 __global__ void __launch_bounds__(kRenderThreads, kSingleRenderBlocks) render_split_kernel(SplitArgs s) {
@@ -367,7 +379,8 @@ cudaError_t launch_render_split(const SplitArgs& a, int grid, cudaStream_t s) {
   int mg = (a.n_slots + 255) / 256;
   mg = mg < 1 ? 1 : (mg > 152 * 8 ? 152 * 8 : mg);
   split_mask_kernel<<<mg, 256, 0, s>>>(a);
-  split_plan_kernel<<<1, kPlanThreads, 0, s>>>(a);
+  split_scan_kernel<<<1, kPlanThreads, 0, s>>>(a);
+  split_emit_kernel<<<mg, 256, 0, s>>>(a);
   cudaError_t e = cudaMemsetAsync(a.work_counter, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
   render_split_kernel<<<grid, kRenderThreads, tf_smem(a.f.n_tf), s>>>(a);
