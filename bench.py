@@ -378,7 +378,8 @@ def main():
               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
               "config": {"workload": WORKLOAD, "volume": [args.n] * 3, "bricks": 8, "virtual_ranks": 8,
                          "image": [W, H], "cameras": len(cams), "parallelism": f"replicas x{world} (views)",
-                         "l2": "inputs larger than L2 (540 MB of bricks per view)"},
+                         "l2": "inputs larger than L2 (540 MB of bricks per view)",
+                         "seeds": {"volume": 2001, "cameras": 2002}},
               "ms_per_frame": elapsed_ms / args.steps,
               "samples_per_frame": total_samples / max(1, args.steps * world),
               "gpu_launches": args.steps,
@@ -412,6 +413,7 @@ def main():
 
         if not args.no_batched and rank == 0:
             result["batched"] = batched_section(ctx, cams, mine, W, H, args, stream, dev, samples_of)
+            result["batched_uneven"] = uneven_batched_section(vol, dev)
 
         if not args.no_adjoint and rank == 0:
             from aloha_gb300 import scenes as S
@@ -556,6 +558,60 @@ def batched_section(ctx, cams, mine, W, H, args, stream, dev, samples_of):
     b.close()
     return {"views": nv, "tile": [tw, th], "ms_batch": ms_graph, "ms_plain_launches": ms_plain,
             "speedup_vs_plain": ms_plain / ms_graph, "gsamples_per_s": samples / (ms_graph * 1e-3) / 1e9}
+
+
+def uneven_batched_section(vol, dev, big=64, small=32):
+    """The batched configuration: the same 512^3 field in uneven 3x2x2 bricks
+    (x cuts 200, 380; y 256; z 300), 64 views at 1024^2 and 32 at 512^2 in one
+    graph-captured persistent launch (autotuned), against the same views as
+    plain aloha_render launches."""
+    import torch
+
+    from aloha_gb300 import abi
+    from aloha_gb300 import scenes as S
+    from aloha_gb300 import volfile as V
+    n = vol.shape[0]
+    descs = S.grid_split((n, n, n), ([n * 200 // 512, n * 380 // 512], [n // 2], [n * 300 // 512]))
+    ctx = abi.Context(dev.index or 0)
+    ctx.set_bricks(descs, [V.brick_voxels(vol, d) for d in descs])
+    ctx.set_transfer_function(S.ramp_tf())
+    ctx.set_ranks(len(descs))
+    ctx.set_params()
+    sizes = [1024] * big + [512] * small
+    cams = [S.orbit_cameras((n, n, n), 1, w, w, seed=3002 + i)[0] for i, w in enumerate(sizes)]
+    stream = torch.cuda.current_stream()
+    fbs = []
+    samples = 0
+    for v, (w, cam) in enumerate(zip(sizes, cams)):
+        ctx.set_camera(v, *cam)
+        ctx.resize(v, w, w)
+        fbs.append(torch.zeros((w, w), dtype=torch.int32, device=dev))
+        ctx.render(v, fbs[-1], stream)
+        samples += ctx.stats().samples
+    b = ctx.batch(list(range(len(sizes))), fbs)
+    tw, th, _ = b.autotune(stream, reps=1)
+
+    def timed(fn, reps=3):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms_batch = timed(lambda: b.launch_graph(stream))
+    ms_plain = timed(lambda: [ctx.render(v, f, stream) for v, f in enumerate(fbs)])
+    b.close()
+    ctx.close()
+    px = sum(w * w for w in sizes)
+    return {"config": f"{n}^3 in {len(descs)} uneven bricks, {big} views at 1024^2 + {small} at 512^2",
+            "tile": [tw, th], "ms_batch": ms_batch, "ms_plain_launches": ms_plain,
+            "speedup_vs_plain": ms_plain / ms_batch, "gsamples_per_s": samples / (ms_batch * 1e-3) / 1e9,
+            "ms_per_megapixel": ms_batch / (px / 2**20)}
 
 
 def large_section(dev, n=1024, size=2048, views=8, k=64):
