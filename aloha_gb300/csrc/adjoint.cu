@@ -79,6 +79,10 @@ __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevVi
     const float mag = fmaxf(fmaxf(fabsf(ray.o[0]) + fabsf(b.lo[0]), fabsf(ray.o[1]) + fabsf(b.lo[1])),
                             fabsf(ray.o[2]) + fabsf(b.lo[2])) + fabsf(t1);
     const float eps = 2e-6f * mag + 1e-4f;
+    float inv_d[3];  // 1 / direction, once per brick (the lookups below reuse it)
+    if (SKIP)
+#pragma unroll
+      for (int ax = 0; ax < 3; ++ax) inv_d[ax] = 1.0f / ray.d[ax];
     float t_cell = t0;  // samples before it lie in a macrocell found non-empty
     while (t < t1 && color.w < a.et_alpha && nb < cap) {
       if (n == max_samples) return n;
@@ -94,7 +98,7 @@ __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevVi
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) {
           const float face = ray.d[ax] > 0.f ? bnd[ax] + (float)kMacro - eps : bnd[ax] + eps;
-          tb = fminf(tb, (face - (ray.o[ax] - b.lo[ax])) * (1.0f / ray.d[ax]));
+          tb = fminf(tb, (face - (ray.o[ax] - b.lo[ax])) * inv_d[ax]);
         }
         if (!__ldg(b.empty + (mz * mny + my) * mnx + mx)) {
           t_cell = tb;
