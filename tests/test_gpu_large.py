@@ -1,12 +1,17 @@
-"""The large configuration at full size: a 1024^3 fp32 blob field in 4x4x4
-chopSuey bricks (64 virtual ranks), 2048^2 frames, forward plus adjoint for
-the transfer function and the density with a checkpoint every 64 samples.
+"""The batched and the large configurations at full size.
 
-The oracle cannot render this in seconds, so these checks use properties
-that hold at any size: the two work divisions of a frame agree bit for bit,
-the differentiable forward quantises to the render, and the adjoint is linear
-in dL/dimage with a density part independent of whether the transfer-function
-gradient is taken.  About 65 GB of device memory.
+Batched: a 512^3 fp32 blob field in uneven 3x2x2 bricks (12 virtual ranks),
+64 views at 1024^2 and 32 at 512^2 in one graph-captured persistent launch.
+Large: a 1024^3 fp32 blob field in 4x4x4 chopSuey bricks (64 virtual ranks),
+2048^2 frames, forward plus adjoint for the transfer function and the density
+with a checkpoint every 64 samples.
+
+The oracle cannot render these in seconds, so these checks use properties
+that hold at any size: a batch equals the same views rendered one by one, the
+two work divisions of a frame agree bit for bit, the differentiable forward
+quantises to the render, and the adjoint is linear in dL/dimage with a
+density part independent of whether the transfer-function gradient is taken.
+About 65 GB of device memory at most.
 """
 import numpy as np
 import pytest
@@ -22,6 +27,43 @@ N, W, K = 1024, 2048, 64
 
 def _rel(a, b):
     return float((a - b).double().norm() / max(float(b.double().norm()), 1e-30))
+
+
+def test_512cube_uneven_bricks_96_views_batched(gpu_ctx_factory):
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    n = 512
+    vol = S.blob_field((n, n, n), 64, (n / 16.0, n / 6.4), seed=2001, device=dev)
+    descs = S.grid_split((n, n, n), ([200, 380], [256], [300]))
+    assert len(descs) == 12
+    ctx = gpu_ctx_factory()
+    ctx.set_bricks(descs, [V.brick_voxels(vol, d) for d in descs])
+    del vol
+    ctx.set_transfer_function(S.ramp_tf())
+    ctx.set_ranks(12)
+    ctx.set_params()
+    sizes = [1024] * 64 + [512] * 32
+    singles, samples = [], 0
+    for v, w in enumerate(sizes):
+        ctx.set_camera(v, *S.orbit_cameras((n, n, n), 1, w, w, seed=3002 + v)[0])
+        ctx.resize(v, w, w)
+        fb = torch.zeros((w, w), dtype=torch.int32, device=dev)
+        ctx.render(v, fb)
+        torch.cuda.synchronize()
+        samples += ctx.stats().samples
+        singles.append(fb)
+    fbs = [torch.full_like(f, -1) for f in singles]
+    b = ctx.batch(list(range(len(sizes))), fbs)
+    b.autotune(reps=1)
+    for f in fbs:
+        f.fill_(-1)
+    b.launch_graph()
+    torch.cuda.synchronize()
+    assert ctx.stats().samples == samples
+    for got, want in zip(fbs, singles):
+        assert torch.equal(got, want)
+    b.close()
+    ctx.close()
 
 
 def test_1024cube_64_bricks_2048px(gpu_ctx_factory):
