@@ -127,9 +127,46 @@ __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevVi
   return n;
 }
 
-// Training forward of one warp's 8 x 4 pixels at (x, y): march, checkpoints,
-// final colour, and the warp-aggregated append of (pixel, segment) items.
-// Returns the lane's sample count.
+// Stores the march state before every K-th sample (evaluated or skipped):
+// colour, t, the brick walk position, tmin, the jitter draw index and the
+// samples already taken in the brick.  The brick loop sets j, tmin, draw.
+struct CheckpointHook {
+  static constexpr bool kActive = true;
+  Checkpoint* ck;
+  uint32_t K, cap;
+  int* overflow;
+  uint32_t left = 0, m = 0;  // samples to the next checkpoint, checkpoints so far
+  int j = 0;
+  float tmin = 0.0f;
+  uint32_t draw = 0;
+  __device__ __forceinline__ void operator()(float t, uint32_t nb, const float4& col) {
+    if (left == 0) {
+      left = K;
+      if (m < cap) {
+        Checkpoint c;
+        c.r = col.x;
+        c.g = col.y;
+        c.b = col.z;
+        c.a = col.w;
+        c.t = t;
+        c.tmin = tmin;
+        c.jd = (uint32_t)j | (draw << 16);
+        c.nb = nb;
+        ck[m] = c;
+      } else {
+        atomicOr(overflow, 1);
+      }
+      ++m;
+    }
+    --left;
+  }
+};
+
+// Training forward of one warp's 8 x 4 pixels at (x, y): the single rank's
+// march (march_rank's brick walk with one draw, through march_brick, so the
+// colour is the render's bit for bit), checkpoints, final colour, and the
+// warp-aggregated append of (pixel, segment) items.  Returns the lane's
+// sample count.
 __device__ __forceinline__ uint32_t train_subtile(const TrainArgs& a, const DevView& v, const float4* tf_s, int x,
                                                   int y, int lane) {
   const bool active = x < v.width && y < v.height;
@@ -139,40 +176,22 @@ __device__ __forceinline__ uint32_t train_subtile(const TrainArgs& a, const DevV
     pixel = (uint32_t)x + (uint32_t)v.width * (uint32_t)y;
     const Ray ray = generate_ray(v, x, y);
     float4 color = make_float4(0.f, 0.f, 0.f, 0.f);
-    Checkpoint* ck = a.ckpt + (size_t)pixel * a.ckpt_cap;
-    const uint32_t K = a.k, cap = a.ckpt_cap;
-    uint32_t left = 0, m = 0;  // samples to the next checkpoint, checkpoints so far
-    // checkpoint before every K-th sample, evaluated or skipped
-    auto checkpoint = [&](float t, const Walk& w, uint32_t nb, const float4& col) {
-      if (left == 0) {
-        left = K;
-        if (m < cap) {
-          Checkpoint c;
-          c.r = col.x;
-          c.g = col.y;
-          c.b = col.z;
-          c.a = col.w;
-          c.t = t;
-          c.tmin = w.tmin;
-          c.jd = (uint32_t)w.j | (w.draw << 16);
-          c.nb = nb;
-          ck[m] = c;
-        } else {
-          atomicOr(a.overflow, 1);
-        }
-        ++m;
-      }
-      --left;
-    };
-    n = walk_samples<true>(a, v, tf_s, ray, pixel, Walk{0, 0.0f, 0u}, 0.f, 0u, false, color, 0xffffffffu,
-                           [&](const DevBrick&, float t, const Walk& w, uint32_t nb, float, float, float,
-                               const StencilOut&, float, const float4&, const float4& col) {
-                             checkpoint(t, w, nb, col);
-                           },
-                           checkpoint);
+    CheckpointHook hook{a.ckpt + (size_t)pixel * a.ckpt_cap, a.k, a.ckpt_cap, a.overflow};
+    const int* __restrict__ rb = rank_bricks(a, v);
+    const int j1 = __ldg(a.sched + v.sched + 2);
+    for (int j = 0; j < j1; ++j) {
+      const DevBrick b = a.bricks[__ldg(rb + j)];
+      float t0, t1;
+      if (!slab(ray, b.space_lo, b.space_hi, hook.tmin, 1e10f, t0, t1)) continue;
+      const float ils = jitter(a.jitter_mode, a.jitter_value, pixel, (uint32_t)a.accum_id, hook.draw++);
+      hook.j = j;
+      n += march_brick(b, tf_s, a.n_tf, ray, t0, t1, ils, a.dt, a.et_alpha, color, hook);
+      hook.tmin = t1 + 1e-20f;
+      if (!(color.w < a.et_alpha)) break;
+    }
     a.final_rgba[pixel] = color;
     if (a.out_rgba) a.out_rgba[pixel] = color;
-    nseg = min((n + K - 1) / K, cap);
+    nseg = min((n + a.k - 1) / a.k, a.ckpt_cap);
   }
   // warp-aggregated append of (pixel, segment) items, ordered by segment then
   // lane so that a backward warp replays neighbouring rays together
@@ -196,7 +215,7 @@ __device__ __forceinline__ uint32_t train_subtile(const TrainArgs& a, const DevV
 
 // Persistent training forward: warps pull 8 x 4 chunks centre-out (as the
 // render does) from the counter at work_count[1].
-__global__ void __launch_bounds__(128) forward_train_kernel(TrainArgs a, int view) {
+__global__ void __launch_bounds__(128, kSingleRenderBlocks) forward_train_kernel(TrainArgs a, int view) {
   extern __shared__ float4 tf_s[];
   load_tf(tf_s, a.tf, a.n_tf);
   __syncthreads();

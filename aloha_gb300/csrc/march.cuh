@@ -208,11 +208,22 @@ __device__ __forceinline__ uint32_t march_cap(float t0, float t1, float dt) {
   return span < 1e8f ? (uint32_t)(span * 2.0f) + 16u : 200000016u;
 }
 
+// A march hook sees every sample, full or skipped, before it is taken: its
+// t, the samples already taken in the brick and the colour so far.  The
+// render passes NoHook; the differentiable forward stores checkpoints.  An
+// active hook keeps `left`, the samples it lets pass before it needs to see
+// one again, so runs of skipped samples only stop where it does.
+struct NoHook {
+  static constexpr bool kActive = false;
+  __device__ __forceinline__ void operator()(float, uint32_t, const float4&) {}
+};
+
 // integrateBrick (deviceCode.cpp:256-298) over [t0, t1); returns the number
 // of samples taken.
+template <class Hook>
 __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
                                                 const Ray& r, float t0, float t1, float ils, float dt, float et,
-                                                float4& color) {
+                                                float4& color, Hook& hook) {
   const float4* __restrict__ base = b.base;
   const int sy = b.sy, sz = b.sz, nx = b.n[0], ny = b.n[1], nz = b.n[2];
   const float lox = b.lo[0], loy = b.lo[1], loz = b.lo[2];
@@ -254,16 +265,35 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
         // Empty macrocell: a sample there has alpha exactly 0 and leaves the
         // colour unchanged, so only t and the sample count advance (the same
         // t += dt sequence as full samples) up to tb; the test resumes there.
+        hook(t, n, color);
         ++n;
         t = t + dt;
-        while (t < tb && n < cap) {
-          ++n;
-          t = t + dt;
+        if constexpr (!Hook::kActive) {
+          while (t < tb && n < cap) {
+            ++n;
+            t = t + dt;
+          }
+        } else {
+          while (t < tb && n < cap) {
+            uint32_t k = hook.left;
+            while (k > 0 && t < tb && n < cap) {
+              ++n;
+              t = t + dt;
+              --k;
+            }
+            hook.left = k;
+            if (k == 0 && t < tb && n < cap) {
+              hook(t, n, color);
+              ++n;
+              t = t + dt;
+            }
+          }
         }
         continue;
       }
       t_cell = tb;
     }
+    hook(t, n, color);
     ++n;
     const StencilOut s = stencil(base, sy, sz, nx, ny, nz, ux, uy, uz);
     const float shade = shade_factor(s, r);
@@ -324,7 +354,8 @@ __device__ __forceinline__ float4 march_rank(const FrameArgs& a, const DevView& 
       const float ils = jitter(a.jitter_mode, a.jitter_value, (uint32_t)pixel, (uint32_t)a.accum_id, draw++);
       const float tnear = (t0 > tmin ? t0 : 0.0f) + tmin;
       z = fminf(z, tnear / v.max_depth);
-      ns += march_brick(b, tf_s, a.n_tf, ray, t0, t1, ils, a.dt, a.et_alpha, color);
+      NoHook none;
+      ns += march_brick(b, tf_s, a.n_tf, ray, t0, t1, ils, a.dt, a.et_alpha, color, none);
       tmin = t1 + 1e-20f;
       if (!(color.w < a.et_alpha)) break;
     }
