@@ -84,6 +84,18 @@ bool is_device_pointer(const void* p) {
   return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
 }
 
+// The device address of page-locked host memory registered with CUDA (e.g.
+// cudaHostAlloc / cudaMallocHost), or null for pageable memory.  Kernels on
+// GB300 write such memory directly over NVLink-C2C.
+void* pinned_device_alias(void* p) {
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return attr.type == cudaMemoryTypeHost ? attr.devicePointer : nullptr;
+}
+
 }  // namespace
 
 struct aloha_ctx {
@@ -884,8 +896,13 @@ int aloha_render(aloha_ctx* c, int view, uint32_t* fb, void* stream) {
   rc = prepare_accum(c, view, s, &a.accum);
   if (rc) return rc;
   const size_t npx = (size_t)v.width * v.height;
+  // A pinned host frame buffer is written by the kernel directly; pageable
+  // host memory goes through a device staging buffer.
   const bool host = !is_device_pointer(fb);
-  if (host) {
+  void* pinned = host ? pinned_device_alias(fb) : nullptr;
+  if (pinned) {
+    a.fb = static_cast<uint32_t*>(pinned);
+  } else if (host) {
     CUDA_TRY(c, c->staging_out.ensure(npx * sizeof(uint32_t)));
     a.fb = static_cast<uint32_t*>(c->staging_out.ptr);
   } else {
@@ -895,6 +912,10 @@ int aloha_render(aloha_ctx* c, int view, uint32_t* fb, void* stream) {
   rc = launch_single(c, a, view, s);
   if (rc) return rc;
   c->samples_valid = true;
+  if (pinned) {
+    CUDA_TRY(c, cudaStreamSynchronize(s));
+    return ALOHA_OK;
+  }
   if (host) return finish_host_output(c, fb, a.fb, npx * sizeof(uint32_t), s);
   return ALOHA_OK;
 }

@@ -157,7 +157,11 @@ int aloha_set_render_split(aloha_ctx* ctx, int mode);
 
 /* Render one view into an RGBA8 frame buffer of width*height uint32
  * (Renderer::render, waikikiRenderer.cpp:1015-1080): all virtual ranks march
- * their bricks and their images are composited in one fused kernel. */
+ * their bricks and their images are composited in one fused kernel.  fb may
+ * be device memory, page-locked host memory (cudaHostAlloc / cudaMallocHost:
+ * the kernel writes it directly) or pageable host memory (copied from a
+ * device staging buffer); with host memory the call returns once the frame
+ * is there. */
 int aloha_render(aloha_ctx* ctx, int view, uint32_t* fb, void* stream);
 
 /* The unfused form: per-rank images after renderFrame's output stage

@@ -314,6 +314,30 @@ def test_batch_equals_single_renders(gpu_ctx_factory):
     assert_same_fb(host[1], singles[1])
 
 
+def test_frame_buffer_kinds(gpu_ctx_factory):
+    """Device, page-locked host (written by the kernel directly) and pageable
+    host frame buffers receive the same frame."""
+    torch = pytest.importorskip("torch")
+    vol, descs, vox, tf = T.chopsuey_scene(48, 8)
+    W, H = 77, 53
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8)
+    for split in (abi.SPLIT_PIXELS, abi.SPLIT_RANKS):
+        ctx.set_render_split(split)
+        for cam in T.cameras((48, 48, 48), 2, W, H, seed=41):
+            ctx.set_camera(0, *cam)
+            ctx.resize(0, W, H)
+            dev = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+            ctx.render(0, dev)
+            torch.cuda.synchronize()
+            pinned = torch.full((H, W), -1, dtype=torch.int32).pin_memory()
+            ctx.render(0, pinned)
+            pageable = np.full((H, W), 7, np.uint32)
+            ctx.render(0, pageable)
+            want = dev.cpu().numpy().view(np.uint32)
+            assert_same_fb(pinned.numpy().view(np.uint32), want)
+            assert_same_fb(pageable, want)
+
+
 def test_device_tensors_as_inputs(gpu_ctx_factory, oracle):
     torch = pytest.importorskip("torch")
     vol, descs, vox, tf = T.chopsuey_scene(32, 2)
