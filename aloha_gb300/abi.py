@@ -24,6 +24,7 @@ JITTER_NONE, JITTER_CONST, JITTER_HASH = 0, 1, 2
 COMPOSITE_FP32, COMPOSITE_UBYTE = 0, 1
 ORDER_FACES, ORDER_REFERENCE_KD = 0, 1
 SPLIT_AUTO, SPLIT_PIXELS, SPLIT_RANKS = 0, 1, 2
+CHUNKS_AUTO, CHUNKS_RING, CHUNKS_PROBED = 0, 1, 2
 
 # Every exported symbol of include/aloha.h (checked by the CPU test suite).
 EXPORTS = [
@@ -34,7 +35,7 @@ EXPORTS = [
     "aloha_composite_over", "aloha_composite_over_rgba8", "aloha_get_stats", "aloha_batch_create",
     "aloha_batch_set_config", "aloha_batch_get_config", "aloha_batch_launch", "aloha_batch_launch_graph",
     "aloha_batch_autotune", "aloha_batch_destroy", "aloha_render_batch", "aloha_forward", "aloha_backward",
-    "aloha_composite_over_noalloc", "aloha_set_render_tile", "aloha_set_render_split",
+    "aloha_composite_over_noalloc", "aloha_set_render_tile", "aloha_set_render_split", "aloha_set_chunk_order",
 ]
 
 
@@ -103,6 +104,7 @@ _SIGS = {
     "aloha_composite_over_noalloc": ([P, P, I, I, I, I, P, P], I),
     "aloha_set_render_tile": ([P, I, I], I),
     "aloha_set_render_split": ([P, I], I),
+    "aloha_set_chunk_order": ([P, I], I),
 }
 
 
@@ -245,6 +247,11 @@ class Context:
     # ---- render
     def set_render_tile(self, tile_w: int, tile_h: int):
         self._check(self._lib.aloha_set_render_tile(self.h, int(tile_w), int(tile_h)))
+
+    def set_chunk_order(self, mode: int):
+        """CHUNKS_AUTO, CHUNKS_RING (centre-out) or CHUNKS_PROBED (most expensive
+        first by a coarse probe); frames are bit-identical."""
+        self._check(self._lib.aloha_set_chunk_order(self.h, int(mode)))
 
     def set_render_split(self, mode: int):
         """SPLIT_AUTO, SPLIT_PIXELS (one thread per pixel over all ranks) or

@@ -17,7 +17,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libaloha_gb300.so")
-SOURCES = ["render.cu", "api.cpp", "order.cpp", "batch.cpp", "adjoint.cu", "noalloc.cu"]
+SOURCES = ["render.cu", "schedule.cu", "api.cpp", "order.cpp", "batch.cpp", "adjoint.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

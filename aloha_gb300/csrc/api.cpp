@@ -134,6 +134,9 @@ struct aloha_ctx {
   // the transfer-function size through shared memory)
   int chunk_w = 0, chunk_h = 0;  // 0 = automatic
   int grid_n_tf = -1, grid_blocks = 0, grid_cw = 0, grid_ch = 0;
+  // cost-ordered chunks of single-view renders: mode, probe costs | max | order
+  int chunk_order_mode = ALOHA_CHUNKS_AUTO;
+  DeviceBuffer chunk_order;
   // rank-split render: mode, scratch rank images, per-chunk tickets, grid
   int split_mode = ALOHA_SPLIT_AUTO;
   DeviceBuffer split_images, split_masks, split_items, split_done;
@@ -445,6 +448,28 @@ int launch_single(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   b.single_view = view;
   b.total_tiles = ring_slots(v.width, v.height, cw, ch);
   b.work_counter = static_cast<unsigned int*>(c->work.ptr);
+  const bool probed = c->chunk_order_mode == ALOHA_CHUNKS_PROBED ||
+                      (c->chunk_order_mode == ALOHA_CHUNKS_AUTO && (long long)v.width * v.height >= 512ll * 512ll);
+  if (probed) {
+    ChunkOrderArgs o{};
+    o.f = f;
+    o.view = view;
+    o.cw = cw;
+    o.ch = ch;
+    o.n_slots = b.total_tiles;
+    const size_t chunks = (size_t)((v.width + cw - 1) / cw) * ((v.height + ch - 1) / ch);
+    const size_t slots = (size_t)o.n_slots, hist = (size_t)kOrderClasses * chunk_order_blocks(o.n_slots);
+    const size_t key_words = (slots + 3) / 4;  // uint8 keys, padded to whole words
+    CUDA_TRY(c, c->chunk_order.ensure((key_words + slots + hist + chunks) * sizeof(uint32_t)));
+    uint32_t* w = static_cast<uint32_t*>(c->chunk_order.ptr);
+    o.key = reinterpret_cast<uint8_t*>(w);
+    o.cid = reinterpret_cast<int*>(w + key_words);
+    o.hist = w + key_words + slots;
+    o.order = reinterpret_cast<int*>(w + key_words + slots + hist);
+    CUDA_TRY(c, launch_chunk_order(o, s));
+    b.chunk_order = o.order;
+    b.total_tiles = (int)chunks;
+  }
   const int warps_per_block = kRenderThreads / 32;
   const int grid = std::max(1, std::min(c->grid_blocks, (b.total_tiles + warps_per_block - 1) / warps_per_block));
   CUDA_TRY(c, cudaMemsetAsync(c->work.ptr, 0, sizeof(unsigned int), s));
@@ -622,7 +647,7 @@ int aloha_destroy(aloha_ctx* c) {
   for (DeviceBuffer* b : {&c->voxels, &c->bricks_dev, &c->staging_in, &c->tf, &c->views_dev, &c->sched_dev,
                           &c->counter, &c->flag, &c->staging_out, &c->mc_ranges, &c->mc_empty, &c->tf_prefix,
                           &c->work, &c->grad4, &c->split_images, &c->split_masks, &c->split_items,
-                          &c->split_done})
+                          &c->split_done, &c->chunk_order})
     b->release();
   delete c;
   return ALOHA_OK;
@@ -874,6 +899,14 @@ int aloha_set_render_tile(aloha_ctx* c, int tile_w, int tile_h) {
                    tile_h);
   c->chunk_w = tile_w;
   c->chunk_h = tile_h;
+  return ALOHA_OK;
+}
+
+int aloha_set_chunk_order(aloha_ctx* c, int mode) {
+  if (!c) return ALOHA_ERR_NULL_POINTER;
+  if (mode != ALOHA_CHUNKS_AUTO && mode != ALOHA_CHUNKS_RING && mode != ALOHA_CHUNKS_PROBED)
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "chunk order %d not AUTO (0), RING (1) or PROBED (2)", mode);
+  c->chunk_order_mode = mode;
   return ALOHA_OK;
 }
 

@@ -82,7 +82,25 @@ struct BatchArgs {
   int single_view;
   int total_tiles;           // chunks in the launch
   unsigned int* work_counter;
+  const int* chunk_order;    // single view: chunk ids in the order to render them, or null (ring order)
 };
+
+// Cost-ordered chunks of one view (schedule.cu): a coarse probe per chunk
+// estimates its cost, and the chunks are sorted stably by cost class, most
+// expensive first, so the frame does not end on a long chunk started last.
+constexpr int kOrderClasses = 64;  // cost classes, a quarter octave apart
+struct ChunkOrderArgs {
+  FrameArgs f;
+  int view;
+  int cw, ch;        // chunk shape
+  int n_slots;       // ring slots of the chunk grid (the probe's input order)
+  uint8_t* key;      // [n_slots] cost class per slot (0xff off the grid)
+  int* cid;          // [n_slots] chunk id per slot
+  uint32_t* hist;    // [kOrderClasses][chunk_order_blocks(n_slots)] counts, then offsets
+  int* order;        // [chunks] chunk ids, most expensive first
+};
+int chunk_order_blocks(int n_slots);
+cudaError_t launch_chunk_order(const ChunkOrderArgs& a, cudaStream_t s);
 
 // Rank-split render of one view into f.fb: work items are (8x4 chunk, rank)
 // pairs for the ranks whose screen rectangle covers the chunk; f.rank_images

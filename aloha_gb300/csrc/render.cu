@@ -48,7 +48,14 @@ __global__ void __launch_bounds__(kRenderThreads, MINB) render_warps_kernel(Batc
     const DevView v = b.f.views[b.view_ids ? __ldg(b.view_ids + item) : b.single_view];
     uint32_t* fb = b.fbs ? b.fbs[item] : b.f.fb;
     int ccx, ccy;
-    if (!ring_chunk(chunk - first, (v.width + CW - 1) / CW, (v.height + CH - 1) / CH, ccx, ccy)) continue;
+    const int cxn = (v.width + CW - 1) / CW;
+    if (b.chunk_order) {
+      const int id = __ldg(b.chunk_order + chunk);
+      ccx = id % cxn;
+      ccy = id / cxn;
+    } else if (!ring_chunk(chunk - first, cxn, (v.height + CH - 1) / CH, ccx, ccy)) {
+      continue;
+    }
     const int x0 = ccx * CW, y0 = ccy * CH;
 #pragma unroll 1
     for (int sub = 0; sub < (CW / 8) * (CH / 4); ++sub) {

@@ -324,12 +324,16 @@ def main():
 
     # work-division sweep of the single-view render (untimed): the pixel split
     # at three chunk shapes, and the (chunk, rank) split
-    schedules = {"pixels 8x4": (abi.SPLIT_PIXELS, 8, 4), "pixels 8x8": (abi.SPLIT_PIXELS, 8, 8),
-                 "pixels 16x8": (abi.SPLIT_PIXELS, 16, 8), "ranks": (abi.SPLIT_RANKS, 0, 0)}
+    schedules = {"pixels 8x4": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_PROBED),
+                 "pixels 8x4 ring order": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_RING),
+                 "pixels 8x8": (abi.SPLIT_PIXELS, 8, 8, abi.CHUNKS_PROBED),
+                 "pixels 16x8": (abi.SPLIT_PIXELS, 16, 8, abi.CHUNKS_PROBED),
+                 "ranks": (abi.SPLIT_RANKS, 0, 0, abi.CHUNKS_AUTO)}
     sched_ms = {}
-    for name, (split, tw, th) in schedules.items():
+    for name, (split, tw, th, chunks) in schedules.items():
         ctx.set_render_split(split)
         ctx.set_render_tile(tw, th)
+        ctx.set_chunk_order(chunks)
         probe = mine[:8]
         for ci in probe[:2]:
             ctx.set_camera(0, *cams[ci])
@@ -345,10 +349,16 @@ def main():
             ms += e0.elapsed_time(e1)
         sched_ms[name] = ms / len(probe)
     best = min(sched_ms, key=sched_ms.get)
-    split, tw, th = schedules[best]
+    split, tw, th, chunks = schedules[best]
     ctx.set_render_split(split)
     ctx.set_render_tile(tw, th)
+    ctx.set_chunk_order(chunks)
     kernel = "render_split_kernel" if split == abi.SPLIT_RANKS else f"render_warps_kernel<{tw},{th}>"
+    # our kernels per frame: the render, plus the chunk probe and sort, or the
+    # rank split's mask, scan and emit
+    probed = split != abi.SPLIT_RANKS and (chunks == abi.CHUNKS_PROBED or
+                                           (chunks == abi.CHUNKS_AUTO and W * H >= 512 * 512))
+    launches_per_frame = 4 if split == abi.SPLIT_RANKS else (3 if probed else 1)
 
     steps = [mine[k % len(mine)] for k in range(args.steps)]
     for k in range(args.warmup):
@@ -389,7 +399,7 @@ def main():
               "config": workload_config(args, len(cams), world),
               "ms_per_frame": elapsed_ms / args.steps,
               "samples_per_frame": total_samples / max(1, args.steps * world),
-              "gpu_launches": args.steps,
+              "gpu_launches": args.steps * launches_per_frame,
               "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                            "frac": achieved / peak, "peak_kind": peak_kind,
                            "traffic": traffic["bytes_per_launch"] if traffic else None,

@@ -47,6 +47,7 @@ enum { ALOHA_JITTER_NONE = 0, ALOHA_JITTER_CONST = 1, ALOHA_JITTER_HASH = 2 };
 enum { ALOHA_COMPOSITE_FP32 = 0, ALOHA_COMPOSITE_UBYTE = 1 };
 enum { ALOHA_ORDER_FACES = 0, ALOHA_ORDER_REFERENCE_KD = 1 };
 enum { ALOHA_SPLIT_AUTO = 0, ALOHA_SPLIT_PIXELS = 1, ALOHA_SPLIT_RANKS = 2 };
+enum { ALOHA_CHUNKS_AUTO = 0, ALOHA_CHUNKS_RING = 1, ALOHA_CHUNKS_PROBED = 2 };
 
 typedef struct aloha_ctx aloha_ctx;
 
@@ -154,6 +155,15 @@ int aloha_set_render_tile(aloha_ctx* ctx, int tile_w, int tile_h);
  * up (when it applies) and the pixel split below.  No reference counterpart
  * (each reference rank is its own process). */
 int aloha_set_render_split(aloha_ctx* ctx, int mode);
+
+/* The order in which warps take the chunks of a single-view render (pixel
+ * split).  ALOHA_CHUNKS_RING: centre-out square rings.  ALOHA_CHUNKS_PROBED:
+ * most expensive first, by a coarse probe of each chunk's centre ray through
+ * the empty-space tables (two small kernels before the render), so that the
+ * frame does not end on a long chunk started late.  Frames are bit-identical
+ * either way.  ALOHA_CHUNKS_AUTO (the default) probes frames of 512^2 pixels
+ * or more.  No reference counterpart. */
+int aloha_set_chunk_order(aloha_ctx* ctx, int mode);
 
 /* Render one view into an RGBA8 frame buffer of width*height uint32
  * (Renderer::render, waikikiRenderer.cpp:1015-1080): all virtual ranks march

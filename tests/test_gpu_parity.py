@@ -152,6 +152,26 @@ def test_rank_split_matches_pixel_split(gpu_ctx_factory, scene):
             assert n_got == n_want
 
 
+@pytest.mark.parametrize("tile", [(8, 4), (16, 8)])
+@pytest.mark.parametrize("chunks", [abi.CHUNKS_RING, abi.CHUNKS_PROBED])
+def test_chunk_order_bit_exact(gpu_ctx_factory, oracle, tile, chunks):
+    """The probed (most expensive first) chunk order renders the same frames
+    and sample counts as the ring order, on ragged frames."""
+    vol, descs, vox, tf = T.chopsuey_scene(48, 8)
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8)
+    ctx.set_render_split(abi.SPLIT_PIXELS)
+    ctx.set_render_tile(*tile)
+    ctx.set_chunk_order(chunks)
+    for (W, H), seed in [((70, 42), 5), ((129, 65), 6)]:
+        cam = T.cameras((48, 48, 48), 1, W, H, seed=seed)[0]
+        fb, samples = gpu_frame(ctx, cam, W, H)
+        ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=8)
+        assert_same_fb(fb, ref["fb"])
+        assert samples == ref["samples"]
+    with pytest.raises(abi.AlohaError):
+        ctx.set_chunk_order(3)
+
+
 def test_rank_split_across_resizes(gpu_ctx_factory, oracle):
     """The per-chunk tickets of the rank split are reset by the kernel itself;
     frames of growing and shrinking size in a row must all stay exact."""
