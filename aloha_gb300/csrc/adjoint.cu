@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(128, kSingleRenderBlocks) forward_train_kernel
   const DevView v = a.views[view];
   const int lane = threadIdx.x & 31;
   const int cxn = (v.width + 7) / 8, cyn = (v.height + 3) / 4;
-  const int total = ring_slots(v.width, v.height, 8, 4);
+  const int total = a.chunk_order ? a.n_chunks : ring_slots(v.width, v.height, 8, 4);
   uint32_t n = 0;
   for (;;) {
     int chunk = 0;
@@ -230,7 +230,13 @@ __global__ void __launch_bounds__(128, kSingleRenderBlocks) forward_train_kernel
     chunk = __shfl_sync(0xffffffffu, chunk, 0);
     if (chunk >= total) break;
     int ccx, ccy;
-    if (!ring_chunk(chunk, cxn, cyn, ccx, ccy)) continue;
+    if (a.chunk_order) {
+      const int id = __ldg(a.chunk_order + chunk);
+      ccx = id % cxn;
+      ccy = id / cxn;
+    } else if (!ring_chunk(chunk, cxn, cyn, ccx, ccy)) {
+      continue;
+    }
     n += train_subtile(a, v, tf_s, ccx * 8 + (lane & 7), ccy * 4 + (lane >> 3), lane);
   }
   count_samples(a.counter, n);

@@ -45,6 +45,8 @@ struct TrainArgs {
   const int4* brick_grid_origin;  // per brick: voxelRange.lower - grid_lo
   int grid_dims[3];
   unsigned long long* counter;
+  const int* chunk_order;     // forward: 8x4 chunk ids in the order to march them, or null (ring order)
+  int n_chunks;               // entries of chunk_order
 };
 
 cudaError_t launch_forward_train(const TrainArgs& a, int view, int width, int height, int max_grid, cudaStream_t s);

@@ -416,6 +416,36 @@ int launch_split(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   return ALOHA_OK;
 }
 
+// The cost-ordered chunk list of a single view when the chunk-order mode asks
+// for one (probe and sort kernels on `s`); *order stays null for ring order.
+int plan_chunk_order(aloha_ctx* c, const FrameArgs& f, int view, int cw, int ch, cudaStream_t s, const int** order,
+                     int* chunks) {
+  const ViewState& v = c->views[view];
+  *order = nullptr;
+  const bool probed = c->chunk_order_mode == ALOHA_CHUNKS_PROBED ||
+                      (c->chunk_order_mode == ALOHA_CHUNKS_AUTO && (long long)v.width * v.height >= 512ll * 512ll);
+  if (!probed) return ALOHA_OK;
+  ChunkOrderArgs o{};
+  o.f = f;
+  o.view = view;
+  o.cw = cw;
+  o.ch = ch;
+  o.n_slots = ring_slots(v.width, v.height, cw, ch);
+  const size_t n_chunks = (size_t)((v.width + cw - 1) / cw) * ((v.height + ch - 1) / ch);
+  const size_t slots = (size_t)o.n_slots, hist = (size_t)kOrderClasses * chunk_order_blocks(o.n_slots);
+  const size_t key_words = (slots + 3) / 4;  // uint8 keys, padded to whole words
+  CUDA_TRY(c, c->chunk_order.ensure((key_words + slots + hist + n_chunks) * sizeof(uint32_t)));
+  uint32_t* w = static_cast<uint32_t*>(c->chunk_order.ptr);
+  o.key = reinterpret_cast<uint8_t*>(w);
+  o.cid = reinterpret_cast<int*>(w + key_words);
+  o.hist = w + key_words + slots;
+  o.order = reinterpret_cast<int*>(w + key_words + slots + hist);
+  CUDA_TRY(c, launch_chunk_order(o, s));
+  *order = o.order;
+  *chunks = (int)n_chunks;
+  return ALOHA_OK;
+}
+
 // One persistent render launch of a single view (resets the work counter).
 int launch_single(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   const ViewState& v = c->views[view];
@@ -448,27 +478,13 @@ int launch_single(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   b.single_view = view;
   b.total_tiles = ring_slots(v.width, v.height, cw, ch);
   b.work_counter = static_cast<unsigned int*>(c->work.ptr);
-  const bool probed = c->chunk_order_mode == ALOHA_CHUNKS_PROBED ||
-                      (c->chunk_order_mode == ALOHA_CHUNKS_AUTO && (long long)v.width * v.height >= 512ll * 512ll);
-  if (probed) {
-    ChunkOrderArgs o{};
-    o.f = f;
-    o.view = view;
-    o.cw = cw;
-    o.ch = ch;
-    o.n_slots = b.total_tiles;
-    const size_t chunks = (size_t)((v.width + cw - 1) / cw) * ((v.height + ch - 1) / ch);
-    const size_t slots = (size_t)o.n_slots, hist = (size_t)kOrderClasses * chunk_order_blocks(o.n_slots);
-    const size_t key_words = (slots + 3) / 4;  // uint8 keys, padded to whole words
-    CUDA_TRY(c, c->chunk_order.ensure((key_words + slots + hist + chunks) * sizeof(uint32_t)));
-    uint32_t* w = static_cast<uint32_t*>(c->chunk_order.ptr);
-    o.key = reinterpret_cast<uint8_t*>(w);
-    o.cid = reinterpret_cast<int*>(w + key_words);
-    o.hist = w + key_words + slots;
-    o.order = reinterpret_cast<int*>(w + key_words + slots + hist);
-    CUDA_TRY(c, launch_chunk_order(o, s));
-    b.chunk_order = o.order;
-    b.total_tiles = (int)chunks;
+  int chunks = 0;
+  const int* order = nullptr;
+  int rc = plan_chunk_order(c, f, view, cw, ch, s, &order, &chunks);
+  if (rc) return rc;
+  if (order) {
+    b.chunk_order = order;
+    b.total_tiles = chunks;
   }
   const int warps_per_block = kRenderThreads / 32;
   const int grid = std::max(1, std::min(c->grid_blocks, (b.total_tiles + warps_per_block - 1) / warps_per_block));
@@ -1171,6 +1187,10 @@ int aloha_forward(aloha_ctx* c, int view, float* rgba, int checkpoint_every, voi
   CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
   const int per_sm = forward_train_blocks_per_sm(c->n_tf);
   if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "forward occupancy query failed");
+  {
+    const int rc = plan_chunk_order(c, frame_args(c), view, 8, 4, s, &a.chunk_order, &a.n_chunks);
+    if (rc) return rc;
+  }
   CUDA_TRY(c, launch_forward_train(a, view, v.width, v.height, per_sm * c->num_sms, s));
   c->samples_valid = true;
   t.valid = true;
