@@ -249,12 +249,14 @@ def test_progressive_accumulation(gpu_ctx_factory, oracle, split):
         assert_same_fb(fb, ref["fb"])
 
 
-@pytest.mark.parametrize("split", SPLITS)
-def test_pathological_cameras(gpu_ctx_factory, oracle, split):
+@pytest.mark.parametrize("split,chunks", [(abi.SPLIT_PIXELS, abi.CHUNKS_RING), (abi.SPLIT_PIXELS, abi.CHUNKS_PROBED),
+                                          (abi.SPLIT_RANKS, abi.CHUNKS_AUTO)])
+def test_pathological_cameras(gpu_ctx_factory, oracle, split, chunks):
     vol, descs, vox, tf = T.chopsuey_scene(32, 8)
     W, H = 40, 40
     ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8)
     ctx.set_render_split(split)
+    ctx.set_chunk_order(chunks)
     cams = [
         S.look_at_camera([16.0, 16.0, 16.0], [40.0, 17.0, 15.0], [0, 1, 0], 60.0, W, H),  # inside, on a face
         S.look_at_camera([16.3, 5.0, 9.0], [16.3, 5.0, -30.0], [0, 1, 0], 30.0, W, H),   # axis-aligned rays
