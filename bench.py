@@ -354,11 +354,12 @@ def main():
     ctx.set_render_tile(tw, th)
     ctx.set_chunk_order(chunks)
     kernel = "render_split_kernel" if split == abi.SPLIT_RANKS else f"render_warps_kernel<{tw},{th}>"
-    # our kernels per frame: the render, plus the chunk probe and sort, or the
-    # rank split's mask, scan and emit
+    # our kernels per frame: the render, plus the chunk probe and the class
+    # histogram, scan and scatter of the cost order, or the rank split's mask,
+    # scan and emit
     probed = split != abi.SPLIT_RANKS and (chunks == abi.CHUNKS_PROBED or
                                            (chunks == abi.CHUNKS_AUTO and W * H >= 512 * 512))
-    launches_per_frame = 4 if split == abi.SPLIT_RANKS else (3 if probed else 1)
+    launches_per_frame = 4 if split == abi.SPLIT_RANKS else (5 if probed else 1)
 
     steps = [mine[k % len(mine)] for k in range(args.steps)]
     for k in range(args.warmup):
