@@ -385,6 +385,9 @@ bool use_rank_split(const aloha_ctx* c, const FrameArgs& f, const ViewState& v) 
   return split_scratch_bytes(c, v) <= kSplitScratchCap;
 }
 
+int plan_chunk_order(aloha_ctx* c, const FrameArgs& f, int view, int cw, int ch, cudaStream_t s, const int** order,
+                     int* chunks, bool auto_order = true);
+
 // Rank-split launch of a single view (mask, plan and render kernels).
 int launch_split(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   const ViewState& v = c->views[view];
@@ -393,6 +396,15 @@ int launch_split(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   a.f = f;
   a.view = view;
   a.n_slots = ring_slots(v.width, v.height, 8, 4);
+  {  // cost order of the 8x4 chunks (positions are then chunks, not ring slots)
+    int chunks = 0;
+    // automatic ordering only below the automatic rank-split range: with many
+    // ranks the (chunk, rank) items are short already (64 bricks at 2048^2:
+    // 6.29 ms in ring order, 6.47 ms cost-ordered)
+    const int rc = plan_chunk_order(c, f, view, 8, 4, s, &a.chunk_order, &chunks, R < kAutoRankSplitRanks);
+    if (rc) return rc;
+    if (a.chunk_order) a.n_slots = chunks;
+  }
   CUDA_TRY(c, c->split_images.ensure((size_t)R * v.width * v.height * sizeof(float4)));
   a.f.rank_images = static_cast<float4*>(c->split_images.ptr);
   CUDA_TRY(c, c->split_masks.ensure((size_t)a.n_slots * (sizeof(unsigned long long) + sizeof(uint32_t))));
@@ -418,12 +430,14 @@ int launch_split(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
 
 // The cost-ordered chunk list of a single view when the chunk-order mode asks
 // for one (probe and sort kernels on `s`); *order stays null for ring order.
+// Automatic mode orders frames of 512^2 pixels or more when auto_order is set.
 int plan_chunk_order(aloha_ctx* c, const FrameArgs& f, int view, int cw, int ch, cudaStream_t s, const int** order,
-                     int* chunks) {
+                     int* chunks, bool auto_order) {
   const ViewState& v = c->views[view];
   *order = nullptr;
   const bool probed = c->chunk_order_mode == ALOHA_CHUNKS_PROBED ||
-                      (c->chunk_order_mode == ALOHA_CHUNKS_AUTO && (long long)v.width * v.height >= 512ll * 512ll);
+                      (c->chunk_order_mode == ALOHA_CHUNKS_AUTO && auto_order &&
+                       (long long)v.width * v.height >= 512ll * 512ll);
   if (!probed) return ALOHA_OK;
   ChunkOrderArgs o{};
   o.f = f;

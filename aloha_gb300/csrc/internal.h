@@ -111,7 +111,8 @@ constexpr uint32_t kSplitBackground = 127u;  // item code of a chunk no rank cov
 struct SplitArgs {
   FrameArgs f;
   int view;
-  int n_slots;                     // ring slots of 8x4 chunks (< 2^25)
+  int n_slots;                     // work positions: ring slots of 8x4 chunks, or chunks when ordered (< 2^25)
+  const int* chunk_order;          // chunk ids by position (cost order), or null (ring order)
   unsigned long long* masks;       // [n_slots] covering ranks per slot
   uint32_t* offsets;               // [n_slots] first item of each slot
   uint32_t* items;                 // [n_slots * max(1, n_ranks)] slot << 7 | rank position

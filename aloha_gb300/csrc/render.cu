@@ -85,6 +85,18 @@ __global__ void __launch_bounds__(kRenderThreads, MINB) render_warps_kernel(Batc
 // the unmarked ranks' images in place, and resets the ticket for the next
 // launch.  No warp waits on another.
 
+// Chunk of work position p: the p-th of the cost order when there is one,
+// else ring slot p (false off the chunk grid).
+__device__ __forceinline__ bool split_chunk(const SplitArgs& s, int p, int cxn, int cyn, int& cx, int& cy) {
+  if (s.chunk_order) {
+    const int id = __ldg(s.chunk_order + p);
+    cx = id % cxn;
+    cy = id / cxn;
+    return true;
+  }
+  return ring_chunk(p, cxn, cyn, cx, cy);
+}
+
 __device__ __forceinline__ bool rect_covers(const int* __restrict__ q, int cx, int cy) {
   return cx >= __ldg(q) && cy >= __ldg(q + 1) && cx <= __ldg(q + 2) && cy <= __ldg(q + 3);
 }
@@ -101,7 +113,7 @@ __global__ void split_mask_kernel(SplitArgs s) {
     int cx, cy;
     unsigned long long m = 0ull;
     uint32_t items = 0;
-    if (ring_chunk(slot, cxn, cyn, cx, cy)) {
+    if (split_chunk(s, slot, cxn, cyn, cx, cy)) {
       for (int k = 0; k < R; ++k)
         if (rect_covers(rects + 4 * __ldg(order + k), cx, cy)) m |= 1ull << k;
       items = m ? (uint32_t)__popcll(m) : 1u;
@@ -156,7 +168,7 @@ __global__ void split_emit_kernel(SplitArgs s) {
   const int cxn = (v.width + 7) / 8, cyn = (v.height + 3) / 4;
   for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < s.n_slots; slot += gridDim.x * blockDim.x) {
     int cx, cy;
-    if (!ring_chunk(slot, cxn, cyn, cx, cy)) continue;
+    if (!split_chunk(s, slot, cxn, cyn, cx, cy)) continue;
     uint32_t at = s.offsets[slot];
     unsigned long long m = s.masks[slot];
     const uint32_t base = (uint32_t)slot << 7;
@@ -194,7 +206,7 @@ __global__ void __launch_bounds__(kRenderThreads, kSingleRenderBlocks) render_sp
     const uint32_t code = __ldg(s.items + item);
     const int slot = (int)(code >> 7), k = (int)(code & 127u);
     int cx, cy;
-    ring_chunk(slot, cxn, cyn, cx, cy);
+    split_chunk(s, slot, cxn, cyn, cx, cy);
     const int x = cx * 8 + (lane & 7), y = cy * 4 + (lane >> 3);
     const bool valid = x < W && y < H;
     const int pixel = x + W * y;

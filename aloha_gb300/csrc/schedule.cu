@@ -1,11 +1,13 @@
-// schedule.cu -- cost-ordered chunks for the single-view render.
+// schedule.cu -- cost-ordered chunks for single-view renders (both work
+// divisions) and the differentiable forward.
 //
 // A frame ends with its slowest chunk (an 8x4 tile whose rays march far
 // through translucent space), so the order in which warps take chunks sets
 // the length of its tail: started last, a long chunk runs on an almost idle
 // GPU.  Longest-first ordering needs the cost before the frame.  A coarse
 // probe gives a good enough estimate: four rays of the chunk (a 2x2 sample),
-// each stepped at 16 samples' stride through every rank's bricks, counting
+// each stepped at 16 samples' stride through the bricks of every rank whose
+// screen rectangle covers it, counting
 // the strides that land in a non-empty macrocell (no voxel loads, no early
 // termination); the chunk's cost is the largest of the four, as a warp runs
 // as long as its longest ray.  The chunks are then sorted stably by cost
@@ -36,9 +38,14 @@ __device__ uint32_t probe_ray(const ChunkOrderArgs& a, const DevView& v, const i
                               const int* __restrict__ rstart, const int* __restrict__ rbricks, int x, int y) {
   const Ray ray = generate_ray(v, x, y);
   const float stride = kProbeStride * a.f.dt;
+  // ranks whose screen rectangle (in 8x4 chunks) misses the pixel cannot be hit
+  const int* __restrict__ rects = a.f.sched + v.rects;
+  const int qx = x >> 3, qy = y >> 2;
   uint32_t c = 0;
   for (int k = 0; k < v.n_ranks; ++k) {
     const int r = __ldg(order + k);
+    const int* q = rects + 4 * r;
+    if (qx < __ldg(q) || qy < __ldg(q + 1) || qx > __ldg(q + 2) || qy > __ldg(q + 3)) continue;
     float tmin = 0.0f;
     for (int j = __ldg(rstart + r); j < __ldg(rstart + r + 1); ++j) {
       const DevBrick b = a.f.bricks[__ldg(rbricks + j)];

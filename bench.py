@@ -357,9 +357,8 @@ def main():
     # our kernels per frame: the render, plus the chunk probe and the class
     # histogram, scan and scatter of the cost order, or the rank split's mask,
     # scan and emit
-    probed = split != abi.SPLIT_RANKS and (chunks == abi.CHUNKS_PROBED or
-                                           (chunks == abi.CHUNKS_AUTO and W * H >= 512 * 512))
-    launches_per_frame = 4 if split == abi.SPLIT_RANKS else (5 if probed else 1)
+    probed = chunks == abi.CHUNKS_PROBED or (chunks == abi.CHUNKS_AUTO and W * H >= 512 * 512)
+    launches_per_frame = (4 if split == abi.SPLIT_RANKS else 1) + (4 if probed else 0)
 
     steps = [mine[k % len(mine)] for k in range(args.steps)]
     for k in range(args.warmup):

@@ -156,13 +156,15 @@ int aloha_set_render_tile(aloha_ctx* ctx, int tile_w, int tile_h);
  * (each reference rank is its own process). */
 int aloha_set_render_split(aloha_ctx* ctx, int mode);
 
-/* The order in which warps take the chunks of a single-view render (pixel
- * split).  ALOHA_CHUNKS_RING: centre-out square rings.  ALOHA_CHUNKS_PROBED:
+/* The order in which warps take the chunks of a single-view render (and of
+ * the rank split's (chunk, rank) items, and of aloha_forward).
+ * ALOHA_CHUNKS_RING: centre-out square rings.  ALOHA_CHUNKS_PROBED:
  * most expensive first, by a coarse probe of each chunk's centre ray through
  * the empty-space tables (two small kernels before the render), so that the
  * frame does not end on a long chunk started late.  Frames are bit-identical
  * either way.  ALOHA_CHUNKS_AUTO (the default) probes frames of 512^2 pixels
- * or more.  No reference counterpart. */
+ * or more, except for the rank split from 32 virtual ranks up (its items are
+ * short already).  No reference counterpart. */
 int aloha_set_chunk_order(aloha_ctx* ctx, int mode);
 
 /* Render one view into an RGBA8 frame buffer of width*height uint32

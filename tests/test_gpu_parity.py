@@ -129,8 +129,9 @@ def _camera_zoo(dims, W, H, seed):
     return cams
 
 
+@pytest.mark.parametrize("chunks", [abi.CHUNKS_RING, abi.CHUNKS_PROBED])
 @pytest.mark.parametrize("scene", ["chopsuey8", "uneven12"])
-def test_rank_split_matches_pixel_split(gpu_ctx_factory, scene):
+def test_rank_split_matches_pixel_split(gpu_ctx_factory, scene, chunks):
     """The rank split skips the ranks whose screen rectangle misses a chunk;
     over many awkward cameras its frames must equal the pixel split's."""
     if scene == "chopsuey8":
@@ -143,6 +144,7 @@ def test_rank_split_matches_pixel_split(gpu_ctx_factory, scene):
     params = [dict(), dict(heat_map=1, heat_map_scale=0.02), dict(crosshair=1, composite_mode=abi.COMPOSITE_UBYTE)]
     for kw in params:
         ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=R, **kw)
+        ctx.set_chunk_order(chunks)
         for cam in _camera_zoo((48, 48, 48), W, H, seed=len(kw)):
             ctx.set_render_split(abi.SPLIT_PIXELS)
             want, n_want = gpu_frame(ctx, cam, W, H)
