@@ -174,6 +174,23 @@ def test_chunk_order_bit_exact(gpu_ctx_factory, oracle, tile, chunks):
         ctx.set_chunk_order(3)
 
 
+@pytest.mark.parametrize("split,chunks", [(abi.SPLIT_PIXELS, abi.CHUNKS_RING), (abi.SPLIT_PIXELS, abi.CHUNKS_PROBED),
+                                          (abi.SPLIT_RANKS, abi.CHUNKS_RING), (abi.SPLIT_RANKS, abi.CHUNKS_PROBED)])
+def test_tiny_and_thin_frames(gpu_ctx_factory, oracle, split, chunks):
+    """Frames of a few pixels or a single row / column: ring slots mostly off
+    the chunk grid, one chunk, partial chunks."""
+    vol, descs, vox, tf = T.chopsuey_scene(32, 8)
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8)
+    ctx.set_render_split(split)
+    ctx.set_chunk_order(chunks)
+    for (W, H), seed in [((1, 1), 1), ((2, 3), 2), ((9, 1), 3), ((1, 17), 4), ((13, 5), 5)]:
+        cam = S.look_at_camera([16.0 + 40.0 * seed % 7, 50.0, -30.0], [16.0, 16.0, 16.0], [0, 1, 0], 20.0, W, H)
+        fb, samples = gpu_frame(ctx, cam, W, H)
+        ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=8)
+        assert_same_fb(fb, ref["fb"])
+        assert samples == ref["samples"]
+
+
 def test_rank_split_across_resizes(gpu_ctx_factory, oracle):
     """The per-chunk tickets of the rank split are reset by the kernel itself;
     frames of growing and shrinking size in a row must all stay exact."""
