@@ -213,8 +213,9 @@ __device__ __forceinline__ uint32_t train_subtile(const TrainArgs& a, const DevV
   return n;
 }
 
-// Persistent training forward: warps pull 8 x 4 chunks centre-out (as the
-// render does) from the counter at work_count[1].
+// Persistent training forward: warps pull 8 x 4 chunks (in cost order when
+// a.chunk_order is set, else centre-out, as the render does) from the counter
+// at work_count[1].
 __global__ void __launch_bounds__(128, kSingleRenderBlocks) forward_train_kernel(TrainArgs a, int view) {
   extern __shared__ float4 tf_s[];
   load_tf(tf_s, a.tf, a.n_tf);

@@ -9,7 +9,8 @@
 namespace aloha {
 
 // Persistent render: every warp pulls CW x CH pixel chunks of the launch's
-// items (views) from one atomic counter, centre-out per view, and renders
+// items (views) from one atomic counter -- a single view in cost order when
+// b.chunk_order is set (schedule.cu), else centre-out per view -- and renders
 // each chunk as 8 x 4-pixel sub-tiles, so the 32 rays of a warp start within
 // a few voxels of each other.  Warps are independent (no barrier after the
 // transfer function is staged): a warp with long rays never holds finished
@@ -78,7 +79,8 @@ __global__ void __launch_bounds__(kRenderThreads, MINB) render_warps_kernel(Batc
 // covers the chunk (bit k = k-th rank in visibility order); no pixel ray of
 // an unmarked rank can enter its bricks, so its image is the output stage of
 // an empty march.  split_scan_kernel and split_emit_kernel list the work items
-// in slot order (centre-out): one per marked rank, or one compositing-only
+// in position order (the cost order when s.chunk_order is set, else the
+// centre-out ring): one per marked rank, or one compositing-only
 // item for a chunk no rank covers.  render_split_kernel marches each item's rank into its
 // image plane; the warp that completes a chunk's last marked rank (a ticket
 // per chunk, taken after a fence) blends the chunk front to back, evaluating
