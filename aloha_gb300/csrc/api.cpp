@@ -407,9 +407,12 @@ int launch_split(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   }
   CUDA_TRY(c, c->split_images.ensure((size_t)R * v.width * v.height * sizeof(float4)));
   a.f.rank_images = static_cast<float4*>(c->split_images.ptr);
-  CUDA_TRY(c, c->split_masks.ensure((size_t)a.n_slots * (sizeof(unsigned long long) + sizeof(uint32_t))));
+  const size_t scan_blocks = ((size_t)a.n_slots + 1023) / 1024;
+  CUDA_TRY(c, c->split_masks.ensure((size_t)a.n_slots * (sizeof(unsigned long long) + sizeof(uint32_t)) +
+                                    scan_blocks * sizeof(uint32_t)));
   a.masks = static_cast<unsigned long long*>(c->split_masks.ptr);
   a.offsets = reinterpret_cast<uint32_t*>(a.masks + a.n_slots);
+  a.block_sums = a.offsets + a.n_slots;
   CUDA_TRY(c, c->split_items.ensure((size_t)a.n_slots * R * sizeof(uint32_t) + 16));
   a.items = static_cast<uint32_t*>(c->split_items.ptr);
   a.n_items = reinterpret_cast<uint32_t*>(static_cast<char*>(c->split_items.ptr) + (size_t)a.n_slots * R * 4);

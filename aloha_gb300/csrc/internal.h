@@ -115,6 +115,7 @@ struct SplitArgs {
   const int* chunk_order;          // chunk ids by position (cost order), or null (ring order)
   unsigned long long* masks;       // [n_slots] covering ranks per slot
   uint32_t* offsets;               // [n_slots] first item of each slot
+  uint32_t* block_sums;            // [ceil(n_slots / 1024)] scan scratch
   uint32_t* items;                 // [n_slots * max(1, n_ranks)] slot << 7 | rank position
   uint32_t* n_items;               // items listed (written by the plan kernel)
   unsigned int* chunk_done;        // [n_slots] tickets, zero between launches

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(kRenderThreads, MINB) render_warps_kernel(Batc
 // split_mask_kernel marks, per chunk slot, the ranks whose screen rectangle
 // covers the chunk (bit k = k-th rank in visibility order); no pixel ray of
 // an unmarked rank can enter its bricks, so its image is the output stage of
-// an empty march.  split_scan_kernel and split_emit_kernel list the work items
+// an empty march.  The scan kernels and split_emit_kernel list the work items
 // in position order (the cost order when s.chunk_order is set, else the
 // centre-out ring): one per marked rank, or one compositing-only
 // item for a chunk no rank covers.  render_split_kernel marches each item's rank into its
@@ -125,18 +125,14 @@ __global__ void split_mask_kernel(SplitArgs s) {
   }
 }
 
-constexpr int kPlanThreads = 1024;
+// Exclusive scan of the per-slot item counts in place, and the item total,
+// in two levels: per-block sums of kScanTile slots, a one-CTA scan of the
+// block sums, then each block scans its tile and adds its base.
+constexpr int kScanBlock = 256, kScanPer = 4, kScanTile = kScanBlock * kScanPer;
 
-// Exclusive scan of the per-slot item counts in place (one CTA; each thread
-// scans a contiguous range) and the item total.
-__global__ void __launch_bounds__(kPlanThreads) split_scan_kernel(SplitArgs s) {
-  __shared__ uint32_t warp_sum[kPlanThreads / 32];
-  const int per = (s.n_slots + kPlanThreads - 1) / kPlanThreads;
-  const int lo = min(s.n_slots, (int)threadIdx.x * per), hi = min(s.n_slots, lo + per);
-  uint32_t count = 0;
-  for (int i = lo; i < hi; ++i) count += s.offsets[i];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  uint32_t incl = count;
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sum, uint32_t& total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t incl = v;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
     const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
@@ -145,22 +141,65 @@ __global__ void __launch_bounds__(kPlanThreads) split_scan_kernel(SplitArgs s) {
   if (lane == 31) warp_sum[wid] = incl;
   __syncthreads();
   if (wid == 0) {
-    uint32_t w = warp_sum[lane];
+    uint32_t w = lane < nw ? warp_sum[lane] : 0u;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const uint32_t o = __shfl_up_sync(0xffffffffu, w, d);
       if (lane >= d) w += o;
     }
-    warp_sum[lane] = w;  // inclusive over warps
+    if (lane < nw) warp_sum[lane] = w;
   }
   __syncthreads();
-  uint32_t at = incl - count + (wid > 0 ? warp_sum[wid - 1] : 0u);
+  total = warp_sum[nw - 1];
+  return incl - v + (wid > 0 ? warp_sum[wid - 1] : 0u);
+}
+
+__global__ void __launch_bounds__(kScanBlock) split_block_sums_kernel(SplitArgs s, uint32_t* sums) {
+  __shared__ uint32_t warp_sum[kScanBlock / 32];
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPer;
+  uint32_t v = 0;
+#pragma unroll
+  for (int i = 0; i < kScanPer; ++i)
+    if (base + i < s.n_slots) v += s.offsets[base + i];
+  uint32_t total;
+  block_exclusive_scan(v, warp_sum, total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// One CTA: exclusive scan of the block sums (contiguous ranges per thread).
+__global__ void __launch_bounds__(1024) split_sums_scan_kernel(SplitArgs s, uint32_t* sums, int n) {
+  __shared__ uint32_t warp_sum[1024 / 32];
+  const int per = (n + 1023) / 1024;
+  const int lo = min(n, (int)threadIdx.x * per), hi = min(n, lo + per);
+  uint32_t v = 0;
+  for (int i = lo; i < hi; ++i) v += sums[i];
+  uint32_t total;
+  uint32_t at = block_exclusive_scan(v, warp_sum, total);
   for (int i = lo; i < hi; ++i) {
-    const uint32_t c = s.offsets[i];
-    s.offsets[i] = at;
+    const uint32_t c = sums[i];
+    sums[i] = at;
     at += c;
   }
-  if (threadIdx.x == kPlanThreads - 1) *s.n_items = at;
+  if (threadIdx.x == 0) *s.n_items = total;
+}
+
+__global__ void __launch_bounds__(kScanBlock) split_tile_scan_kernel(SplitArgs s, const uint32_t* sums) {
+  __shared__ uint32_t warp_sum[kScanBlock / 32];
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPer;
+  uint32_t c[kScanPer], v = 0;
+#pragma unroll
+  for (int i = 0; i < kScanPer; ++i) {
+    c[i] = base + i < s.n_slots ? s.offsets[base + i] : 0u;
+    v += c[i];
+  }
+  uint32_t total;
+  uint32_t at = block_exclusive_scan(v, warp_sum, total) + sums[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < kScanPer; ++i)
+    if (base + i < s.n_slots) {
+      s.offsets[base + i] = at;
+      at += c[i];
+    }
 }
 
 // Writes each slot's items at its offset: slot << 7 | rank position, or the
@@ -400,7 +439,10 @@ cudaError_t launch_render_split(const SplitArgs& a, int grid, cudaStream_t s) {
   int mg = (a.n_slots + 255) / 256;
   mg = mg < 1 ? 1 : (mg > 152 * 8 ? 152 * 8 : mg);
   split_mask_kernel<<<mg, 256, 0, s>>>(a);
-  split_scan_kernel<<<1, kPlanThreads, 0, s>>>(a);
+  const int tiles = (a.n_slots + kScanTile - 1) / kScanTile;
+  split_block_sums_kernel<<<tiles, kScanBlock, 0, s>>>(a, a.block_sums);
+  split_sums_scan_kernel<<<1, 1024, 0, s>>>(a, a.block_sums, tiles);
+  split_tile_scan_kernel<<<tiles, kScanBlock, 0, s>>>(a, a.block_sums);
   split_emit_kernel<<<mg, 256, 0, s>>>(a);
   cudaError_t e = cudaMemsetAsync(a.work_counter, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
