@@ -47,14 +47,14 @@ __device__ __forceinline__ const int* rank_bricks(const TrainArgs& a, const DevV
 // arithmetic are those of render_pixel / march_brick.
 //
 // With SKIP, samples in empty macrocells (transfer-function alpha exactly 0,
-// see march_brick) are not evaluated: `skipped` is called for each of them
-// instead of `visit`, with the unchanged colour.  The backward replay cannot
-// skip: a zero-alpha sample still carries a gradient for the alpha entries.
-template <bool SKIP, class Visit, class Skipped>
+// see march_brick) are counted and stepped over without a `visit` (in one
+// jump when the steps are exact).  Only the density gradient may skip them: a
+// zero-alpha sample still carries a gradient for the alpha entries.
+template <bool SKIP, class Visit>
 __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevView& v, const float4* tf_s,
                                                  const Ray& ray, uint32_t pixel, Walk w, float t_resume,
                                                  uint32_t nb0, bool resume, float4& color, uint32_t max_samples,
-                                                 Visit visit, Skipped skipped) {
+                                                 Visit visit) {
   const int* __restrict__ rb = rank_bricks(a, v);
   const int j1 = __ldg(a.sched + v.sched + 2);
   const float nf = (float)a.n_tf;
@@ -75,14 +75,18 @@ __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevVi
       t = first_sample_t(t0, dt, ils);
     }
     const uint32_t cap = march_cap(t0, t1, dt);
+    const bool exact = SKIP && exact_steps(t, t1, dt);
     const int mnx = (b.n[0] + kMacro - 1) >> kMacroShift, mny = (b.n[1] + kMacro - 1) >> kMacroShift;
     const float mag = fmaxf(fmaxf(fabsf(ray.o[0]) + fabsf(b.lo[0]), fabsf(ray.o[1]) + fabsf(b.lo[1])),
                             fabsf(ray.o[2]) + fabsf(b.lo[2])) + fabsf(t1);
     const float eps = 2e-6f * mag + 1e-4f;
     float inv_d[3];  // 1 / direction, once per brick (the lookups below reuse it)
-    if (SKIP)
+    float inv_dt = 0.0f;
+    if (SKIP) {
 #pragma unroll
       for (int ax = 0; ax < 3; ++ax) inv_d[ax] = 1.0f / ray.d[ax];
+      inv_dt = 1.0f / dt;
+    }
     float t_cell = t0;  // samples before it lie in a macrocell found non-empty
     while (t < t1 && color.w < a.et_alpha && nb < cap) {
       if (n == max_samples) return n;
@@ -102,9 +106,14 @@ __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevVi
         }
         if (!__ldg(b.empty + (mz * mny + my) * mnx + mx)) {
           t_cell = tb;
+        } else if (exact) {
+          const uint32_t k = run_steps(t, tb, dt, inv_dt, 1u, min(cap - nb, max_samples - n));
+          t = fmaf((float)k, dt, t);
+          n += k;
+          nb += k;
+          continue;
         } else {
           do {
-            skipped(t, w, nb, color);
             ++n;
             ++nb;
             t = t + dt;
@@ -462,8 +471,7 @@ __global__ void __launch_bounds__(128, 5) backward_kernel(TrainArgs a, int view)
             const float ki = kk * inv, kc3 = kk * c3;
             stencil_backward(b, a, __ldg(rb + wcur.j), ux, uy, uz, dv, fmaf(ki, ray.d[0], -kc3 * ex),
                              fmaf(ki, ray.d[1], -kc3 * ey), fmaf(ki, ray.d[2], -kc3 * ez));
-          },
-          [](float, const Walk&, uint32_t, const float4&) {});
+          });
       if (WITH_TF) flush_tf(dtf_s, a.n_tf, pend_i, pend);
     }
   }

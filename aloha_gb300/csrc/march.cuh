@@ -19,6 +19,7 @@
 #include <stdint.h>
 
 #include "internal.h"
+#include "steps.h"
 
 namespace aloha {
 
@@ -77,14 +78,6 @@ __device__ __forceinline__ bool slab(const Ray& r, const float lo[3], const floa
   t0 = fmaxf(tmin, fmaxf(fmaxf(nr[0], nr[1]), nr[2]));
   t1 = fminf(tmax, fminf(fminf(fr[0], fr[1]), fr[2]));
   return t0 < t1;
-}
-
-// firstSampleT (deviceCode.cpp:245-254).
-__device__ __forceinline__ float first_sample_t(float lower, float dt, float ils) {
-  const float n = floorf((lower - dt * ils) / dt);
-  float t = dt * (ils + n);
-  if (t < lower) t = t + dt;
-  return t;
 }
 
 // Seven-tap stencil at voxel coordinate (ux, uy, uz) of a padded brick.
@@ -200,14 +193,6 @@ __device__ __forceinline__ void composite_step(float4& color, const float4 c, fl
   color.w = fmaf(oma, c.w, color.w);
 }
 
-// Iteration cap of one brick march: twice the lattice points in [t0, t1) plus
-// 16.  It never binds while t advances by about dt; it ends the loop when
-// t + dt rounds back to t (ray parameters beyond ~2^24 dt).
-__device__ __forceinline__ uint32_t march_cap(float t0, float t1, float dt) {
-  const float span = (t1 - t0) / dt;
-  return span < 1e8f ? (uint32_t)(span * 2.0f) + 16u : 200000016u;
-}
-
 // A march hook sees every sample, full or skipped, before it is taken: its
 // t, the samples already taken in the brick and the colour so far.  The
 // render passes NoHook; the differentiable forward stores checkpoints.  An
@@ -241,6 +226,8 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
   const float eps = 2e-6f * mag + 1e-4f;
   uint32_t n = 0;
   float t = first_sample_t(t0, dt, ils);
+  const bool exact = exact_steps(t, t1, dt);
+  const float inv_dt = 1.0f / dt;
   // Samples before t_cell lie in the last macrocell found non-empty, so they
   // need no lookup.  Only the skip below depends on the lookup (a full sample
   // in an empty macrocell leaves the colour unchanged as well), so the bound
@@ -265,15 +252,42 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
         // Empty macrocell: a sample there has alpha exactly 0 and leaves the
         // colour unchanged, so only t and the sample count advance (the same
         // t += dt sequence as full samples) up to tb; the test resumes there.
-        hook(t, n, color);
-        ++n;
-        t = t + dt;
+        // The first is always taken.  With exact steps the run is one jump
+        // (or one per checkpoint the hook needs).
         if constexpr (!Hook::kActive) {
+          if (exact) {
+            const uint32_t k = run_steps(t, tb, dt, inv_dt, 1u, cap - n);
+            t = fmaf((float)k, dt, t);
+            n += k;
+            continue;
+          }
+          ++n;
+          t = t + dt;
           while (t < tb && n < cap) {
             ++n;
             t = t + dt;
           }
+        } else if (exact) {
+          hook(t, n, color);
+          ++n;
+          t = t + dt;
+          uint32_t rest = run_steps(t, tb, dt, inv_dt, 0u, cap - n);
+          while (rest > 0u) {
+            const uint32_t take = min(rest, hook.left);
+            t = fmaf((float)take, dt, t);
+            n += take;
+            hook.left -= take;
+            rest -= take;
+            if (rest == 0u) break;
+            hook(t, n, color);
+            ++n;
+            t = t + dt;
+            --rest;
+          }
         } else {
+          hook(t, n, color);
+          ++n;
+          t = t + dt;
           while (t < tb && n < cap) {
             uint32_t k = hook.left;
             while (k > 0 && t < tb && n < cap) {
