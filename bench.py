@@ -32,8 +32,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Gsamples/s & ms/frame (fwd; fwd+adjoint) 512³ DVR @1024² on 1 GB300 vs plain"
-WORKLOAD = ("sort-last DVR: 512^3 fp32 64-blob field, chopSuey 2x2x2 (8 bricks, 8 virtual ranks), "
-            "1024x1024, 256 orbit cameras, dt 0.5, ET 0.99, fp32 ordered-over composite")
+WORKLOAD = ("sort-last DVR: {n}^3 fp32 64-blob field, chopSuey 2x2x2 (8 bricks, 8 virtual ranks), "
+            "{size}x{size}, {cams} orbit cameras, dt 0.5, ET 0.99, fp32 ordered-over composite")
 DEVVIEW_BYTES = 80
 
 
@@ -208,9 +208,14 @@ def cpu_render_sample(descs, vox_np, tf, cams, W, H, target_s, threads=0, max_vi
 
 def workload_config(args, n_cams, world):
     """The config dict of the workload, shared by both arms."""
-    return {"workload": WORKLOAD, "volume": [args.n] * 3, "bricks": 8, "virtual_ranks": 8,
-            "image": [args.size, args.size], "cameras": n_cams, "parallelism": f"replicas x{world} (views)",
-            "l2": "inputs larger than L2 (540 MB of bricks per view)", "seeds": {"volume": 2001, "cameras": 2002}}
+    from aloha_gb300 import volfile as V
+    descs = V.chopsuey_split((args.n,) * 3, 8)
+    brick_mb = algorithmic_bytes(descs, range(len(descs)), 0, 0, 0) / 1e6
+    return {"workload": WORKLOAD.format(n=args.n, size=args.size, cams=n_cams), "volume": [args.n] * 3,
+            "bricks": 8, "virtual_ranks": 8, "image": [args.size, args.size], "cameras": n_cams,
+            "parallelism": f"replicas x{world} (views)",
+            "l2": f"inputs {'larger' if brick_mb > 129 else 'smaller'} than L2 ({brick_mb:.0f} MB of bricks per view)",
+            "seeds": {"volume": 2001, "cameras": 2002}}
 
 
 def reference_arm(args):
