@@ -1,6 +1,6 @@
 """ctypes binding of the CPU oracle (``liboracle.so``).
 
-TEST INFRASTRUCTURE ONLY.  The oracle is the checker: ``tests/``,
+TEST INFRASTRUCTURE ONLY.  The oracle is what results are compared against: ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline arm may load it;
 the product package ``aloha_gb300`` never imports it.
 
