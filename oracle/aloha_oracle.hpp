@@ -107,7 +107,7 @@ template <class R> inline int to_int(R f) {
 template <class R> inline R clamp01(R x) { return std::fmin(std::fmax(x, R(0)), R(1)); }
 
 // make_rgba for one channel (owl's make_rgba is not in the reference tree;
-// this build rounds to nearest).
+// the value is rounded to nearest here and in the kernels).
 template <class R> inline uint32_t quantize8(R x) {
   R c = clamp01(x);
   return (uint32_t)(c * R(255) + R(0.5));
@@ -126,7 +126,8 @@ inline uint32_t pcg_hash(uint32_t v) {
 
 // Per-brick jitter offset ils_t0 in [0,1).  The reference draws it from owl's
 // LCG<4>(pixelID, accumID) (deviceCode.cpp:12,354,386), which is not in the
-// reference tree; this build uses a documented hash of (pixel, accumID, draw).
+// reference tree; the oracle and the kernels use a documented hash of
+// (pixel, accumID, draw) instead.
 inline float jitter_hash(uint32_t pixel, uint32_t accum_id, uint32_t draw) {
   uint32_t h = pcg_hash(pixel ^ pcg_hash(accum_id ^ pcg_hash(draw)));
   return (float)(h >> 8) * (1.0f / 16777216.0f);
