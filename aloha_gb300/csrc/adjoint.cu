@@ -107,10 +107,10 @@ __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevVi
         if (!__ldg(b.empty + (mz * mny + my) * mnx + mx)) {
           t_cell = tb;
         } else if (exact) {
-          const uint32_t k = run_steps(t, tb, dt, inv_dt, 1u, min(cap - nb, max_samples - n));
-          t = fmaf((float)k, dt, t);
-          n += k;
-          nb += k;
+          ++n;
+          ++nb;
+          t = t + dt;
+          n += run_steps(t, nb, tb, cap, dt, inv_dt, max_samples - n);
           continue;
         } else {
           do {

@@ -252,17 +252,15 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
         // Empty macrocell: a sample there has alpha exactly 0 and leaves the
         // colour unchanged, so only t and the sample count advance (the same
         // t += dt sequence as full samples) up to tb; the test resumes there.
-        // The first is always taken.  With exact steps the run is one jump
-        // (or one per checkpoint the hook needs).
+        // The first is always taken.  With exact steps the rest of the run is
+        // a jump per binade crossed (and per checkpoint the hook needs).
         if constexpr (!Hook::kActive) {
-          if (exact) {
-            const uint32_t k = run_steps(t, tb, dt, inv_dt, 1u, cap - n);
-            t = fmaf((float)k, dt, t);
-            n += k;
-            continue;
-          }
           ++n;
           t = t + dt;
+          if (exact) {
+            run_steps(t, n, tb, cap, dt, inv_dt, 0xffffffffu);
+            continue;
+          }
           while (t < tb && n < cap) {
             ++n;
             t = t + dt;
@@ -271,18 +269,12 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
           hook(t, n, color);
           ++n;
           t = t + dt;
-          uint32_t rest = run_steps(t, tb, dt, inv_dt, 0u, cap - n);
-          while (rest > 0u) {
-            const uint32_t take = min(rest, hook.left);
-            t = fmaf((float)take, dt, t);
-            n += take;
-            hook.left -= take;
-            rest -= take;
-            if (rest == 0u) break;
-            hook(t, n, color);
+          for (;;) {
+            hook.left -= run_steps(t, n, tb, cap, dt, inv_dt, hook.left);
+            if (!(t < tb && n < cap)) break;
+            hook(t, n, color);  // a checkpoint falls due here (hook.left == 0)
             ++n;
             t = t + dt;
-            --rest;
           }
         } else {
           hook(t, n, color);

@@ -2,12 +2,13 @@
 // runs of steps (host and device).
 //
 // The march advances t by the rounded sequence t, t+dt, (t+dt)+dt, ...
-// (integrateBrick, deviceCode.cpp:271-296).  If t and dt are both multiples
-// of 2^q and every t the march reaches stays below 2^(24+q) in magnitude,
-// every t + dt is a float (a multiple of 2^q with at most 24 significant
-// bits), so the rounded sequence equals the exact one, and fmaf(k, dt, t)
-// (exact for the same reason) lands on the k-th step directly.  A run of k
-// skipped samples then costs a few instructions instead of k loop trips.
+// (integrateBrick, deviceCode.cpp:271-296).  Every float in a binade
+// [2^e, 2^(e+1)) is a multiple of its spacing 2^(e-23); if dt is a multiple
+// of it too, t + dt is exact while it stays in the binade (or lands on
+// 2^(e+1)), and fmaf(j, dt, t) -- exact for the same reason -- lands on the
+// j-th step directly.  Only the step that crosses a power of two can round.
+// A run of k skipped samples then costs a few instructions per binade it
+// crosses instead of k loop trips.
 //
 // Host-compilable so that the CPU tests can compare the jump with the loop.
 #pragma once
@@ -46,6 +47,12 @@ ALOHA_HD uint32_t float_bits(float x) {
   return b;
 }
 
+ALOHA_HD float bits_float(uint32_t b) {
+  float x;
+  memcpy(&x, &b, sizeof x);
+  return x;
+}
+
 // Largest q with x a multiple of 2^q (x finite; 1000 for 0).
 ALOHA_HD int low_bit_exp(float x) {
   const uint32_t b = float_bits(x) & 0x7fffffffu;
@@ -60,26 +67,56 @@ ALOHA_HD int low_bit_exp(float x) {
   return (e ? e : 1) - 150 + tz;
 }
 
-// True when the steps from t_first (>= 0) up to t1 + dt are exact, with at
-// most 2^22 of them (so step counts convert to float exactly).
+// True when dt is a multiple of the float spacing of every t the march of a
+// brick reaches (all below t1 + dt, above t_first >= 0): then t + dt is exact
+// for every t in a binade [2^e, 2^(e+1)) as long as it stays at or below
+// 2^(e+1), whatever the low bits of t.  Also bounds the brick to 2^22 steps,
+// so step counts convert to float exactly.
 ALOHA_HD bool exact_steps(float t_first, float t1, float dt) {
   if (!(dt > 0.0f) || !(t_first >= 0.0f) || !((t1 - t_first) < 4194304.0f * dt)) return false;
-  const int qt = low_bit_exp(t_first), qd = low_bit_exp(dt);
-  const int q = qt < qd ? qt : qd;
-  const float hi = t1 + 2.0f * dt;  // above every t reached (the last is below t1 + dt)
+  const float hi = t1 + 2.0f * dt;  // above every t reached
   if (!(hi < 3.0e38f)) return false;
-  const int e = (int)((float_bits(hi) >> 23) & 0xffu) - 127;  // hi < 2^(e+1)
-  return e + 1 <= 24 + q;
+  const int e = (int)((float_bits(hi) >> 23) & 0xffu) - 127;  // every t reached is below 2^(e+1)
+  return e - 23 <= low_bit_exp(dt);
 }
 
-// Smallest k in [lo, lim] with t + k dt >= tb (lim if there is none), for
-// exact steps: an estimate from the division, corrected with exact compares.
-ALOHA_HD uint32_t run_steps(float t, float tb, float dt, float inv_dt, uint32_t lo, uint32_t lim) {
-  if (lim <= lo) return lim;
-  const float kf = fminf(fmaxf(ceilf((tb - t) * inv_dt), (float)lo), 4194304.0f);
-  uint32_t k = (uint32_t)kf < lim ? (uint32_t)kf : lim;
-  while (k > lo && !(fmaf((float)(k - 1u), dt, t) < tb)) --k;
-  while (k < lim && fmaf((float)k, dt, t) < tb) ++k;
+// Advances (t, n) like the loop
+//   while (k < max_steps && t < tb && n < cap) { ++n; t = t + dt; ++k; }
+// and returns k, for t > 0 on a brick with exact_steps.  Within t's binade,
+// up to its upper end B = 2^(e+1), the steps are exact, so fmaf(j, dt, t)
+// lands on the j-th one; the step that crosses B may round and is taken as
+// the loop takes it.  One pass per binade crossed.
+ALOHA_HD uint32_t run_steps(float& t, uint32_t& n, float tb, uint32_t cap, float dt, float inv_dt,
+                            uint32_t max_steps) {
+  uint32_t k = 0;
+  while (k < max_steps && t < tb && n < cap) {
+    const uint32_t lim = (max_steps - k) < (cap - n) ? (max_steps - k) : (cap - n);
+    const float B = bits_float((float_bits(t) & 0x7f800000u) + 0x00800000u);  // 2^(e+1)
+    const float d = t - B;  // exact (B/2 <= t < B), <= 0
+    // jb: the most steps that stay at or below B (fmaf(j, dt, d) <= 0 has the sign of the exact value)
+    float jf = fminf(fmaxf(floorf(-d * inv_dt), 0.0f), 4194304.0f);
+    uint32_t jb = (uint32_t)jf < lim ? (uint32_t)jf : lim;
+    while (jb > 0u && fmaf((float)jb, dt, d) > 0.0f) --jb;
+    while (jb < lim && fmaf((float)(jb + 1u), dt, d) <= 0.0f) ++jb;
+    if (jb > 0u && !(fmaf((float)jb, dt, t) < tb)) {
+      // tb is reached within the binade: the first step at or past it
+      float kf = fminf(fmaxf(ceilf((tb - t) * inv_dt), 1.0f), (float)jb);
+      uint32_t j = (uint32_t)kf;
+      while (j > 1u && !(fmaf((float)(j - 1u), dt, t) < tb)) --j;
+      while (j < jb && fmaf((float)j, dt, t) < tb) ++j;
+      t = fmaf((float)j, dt, t);
+      n += j;
+      return k + j;
+    }
+    t = fmaf((float)jb, dt, t);
+    n += jb;
+    k += jb;
+    if (jb == lim) break;
+    // the next step leaves the binade (t < tb, n < cap, k < max_steps still hold)
+    t = t + dt;
+    ++n;
+    ++k;
+  }
   return k;
 }
 

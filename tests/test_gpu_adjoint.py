@@ -107,6 +107,46 @@ def test_density_only_backward(gpu_ctx_factory, oracle, bricks):
     np.testing.assert_allclose(only_den, full_den, rtol=1e-4, atol=1e-6 * float(np.abs(full_den).max()))
 
 
+@pytest.mark.parametrize("kw", [dict(jitter_mode=abi.JITTER_CONST, jitter_value=0.37), dict(dt=0.3),
+                                dict(jitter_mode=abi.JITTER_HASH, dt=0.375)])
+def test_inexact_step_sequences(gpu_ctx_factory, oracle, kw):
+    """Jittered first samples and step sizes that are not powers of two make
+    the t sequence inexact on most bricks, so the training forward and the
+    density-only replay step their skipped runs sample by sample; the dt 0.375
+    case mixes both.  Forward, checkpoints (through the gradients) and both
+    backward forms must still match the oracle."""
+    n = 48
+    vol, descs, vox = density_scene(n, seed=11, bricks=8)
+    tf = S.ramp_tf()
+    W, H = 72, 64
+    ctx = setup(gpu_ctx_factory, descs, vox, tf, **kw)
+    params = oracle.make_params(**kw)
+    rng = np.random.default_rng(41)
+    dtf = np.zeros((tf.shape[0], 4), np.float32)
+    dden = np.zeros((n, n, n), np.float32)
+    only_den = np.zeros((n, n, n), np.float32)
+    ref_tf = np.zeros((tf.shape[0], 4))
+    ref_den = np.zeros((n, n, n))
+    for v, cam in enumerate(T.cameras((n, n, n), 2, W, H, seed=43)):
+        ctx.set_camera(v, *cam)
+        ctx.resize(v, W, H)
+        img = np.zeros((H, W, 4), np.float32)
+        ctx.forward(v, img, 7)
+        ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H, params, n_ranks=1, want=("final",))
+        np.testing.assert_array_equal(img, ref["final"])
+        assert ctx.stats().samples == ref["samples"]
+        dl = rng.uniform(-1, 1, (H, W, 4)).astype(np.float32)
+        ctx.backward(v, dl, dtf, dden, (0, 0, 0), (n, n, n))
+        ctx.backward(v, dl, None, only_den, (0, 0, 0), (n, n, n))
+        r = oracle.adjoint(descs, vox, tf, oracle.make_camera(*cam), W, H, dl, (0, 0, 0), (n, n, n), params)
+        ref_tf += r["dtf"]
+        ref_den += r["ddensity"]
+    assert rel_err(dtf, ref_tf) < 1e-3
+    assert rel_err(dden, ref_den) < 1e-3
+    assert rel_err(only_den, ref_den) < 1e-3
+    assert np.count_nonzero(dden) > 1000
+
+
 def _loss(ctx, views, W, H, weights):
     total = 0.0
     for v in views:

@@ -233,8 +233,11 @@ def test_reference_kd_order_mode(gpu_ctx_factory, oracle):
     dict(island_id=1, num_islands=3),
     dict(jitter_mode=abi.JITTER_NONE),
     dict(jitter_mode=abi.JITTER_CONST, jitter_value=0.37),
+    dict(jitter_mode=abi.JITTER_HASH),
     dict(dt=2.0),
     dict(dt=0.25, et_alpha=0.5),
+    dict(dt=0.375),
+    dict(dt=0.3),
     dict(accum_id=0, crosshair=1, spp=2, composite_mode=abi.COMPOSITE_UBYTE),
 ])
 @pytest.mark.parametrize("split", SPLITS)
