@@ -2,13 +2,15 @@
 loop it replaces.
 
 The kernels step t by the rounded sequence t, t+dt, ... (integrateBrick,
-deviceCode.cpp:271-296).  Where the steps of a brick are exact (t and dt
-multiples of 2^q, every t below 2^(24+q)), a run of samples in an empty
-macrocell is taken in one jump, k = the first step at or past the macrocell's
-exit, t = fmaf(k, dt, t).  tests/cpp/exact_steps_check.cpp compiles the very
-header the kernels use (aloha_gb300/csrc/steps.h) for the host and compares
-jump and loop, bit for bit, on random bricks; the GPU parity tests then pin
-whole frames and sample counts to the oracle, which keeps the loop.
+deviceCode.cpp:271-296).  Inside a binade [2^e, 2^(e+1)) every float is a
+multiple of 2^(e-23); when dt is too, each t + dt is exact until t crosses
+the next power of two, so a run of samples in an empty macrocell is taken as
+jumps t = fmaf(j, dt, t) to the binade's end, the crossing step as the loop
+takes it, and so on to the macrocell's exit.  tests/cpp/exact_steps_check.cpp
+compiles the very header the kernels use (aloha_gb300/csrc/steps.h) for the
+host and compares jump and loop, bit for bit, on random bricks; the GPU
+parity tests then pin whole frames and sample counts to the oracle, which
+keeps the loop.
 """
 import os
 import shutil
@@ -31,4 +33,4 @@ def test_jump_equals_loop(tmp_path):
     fields = out.stdout.split()
     stats = dict(zip(fields[0::2], (int(v) for v in fields[1::2])))
     assert stats["mismatches"] == 0
-    assert stats["jumped"] > 10**6 and stats["exact"] > stats["bricks"] // 4
+    assert stats["jumped"] > 10**6 and stats["exact"] > stats["bricks"] // 4 and stats["crossings"] > 1000
