@@ -85,34 +85,36 @@ ALOHA_HD bool exact_steps(float t_first, float t1, float dt) {
 // and returns k, for t > 0 on a brick with exact_steps.  Within t's binade,
 // up to its upper end B = 2^(e+1), the steps are exact, so fmaf(j, dt, t)
 // lands on the j-th one; the step that crosses B may round and is taken as
-// the loop takes it.  One pass per binade crossed.
+// the loop takes it.  A run that ends inside the binade (the common case)
+// costs one estimate and one check; one that crosses B, a pass per binade.
 ALOHA_HD uint32_t run_steps(float& t, uint32_t& n, float tb, uint32_t cap, float dt, float inv_dt,
                             uint32_t max_steps) {
   uint32_t k = 0;
   while (k < max_steps && t < tb && n < cap) {
     const uint32_t lim = (max_steps - k) < (cap - n) ? (max_steps - k) : (cap - n);
-    const float B = bits_float((float_bits(t) & 0x7f800000u) + 0x00800000u);  // 2^(e+1)
-    const float d = t - B;  // exact (B/2 <= t < B), <= 0
-    // jb: the most steps that stay at or below B (fmaf(j, dt, d) <= 0 has the sign of the exact value)
-    float jf = fminf(fmaxf(floorf(-d * inv_dt), 0.0f), 4194304.0f);
-    uint32_t jb = (uint32_t)jf < lim ? (uint32_t)jf : lim;
-    while (jb > 0u && fmaf((float)jb, dt, d) > 0.0f) --jb;
-    while (jb < lim && fmaf((float)(jb + 1u), dt, d) <= 0.0f) ++jb;
-    if (jb > 0u && !(fmaf((float)jb, dt, t) < tb)) {
-      // tb is reached within the binade: the first step at or past it
-      float kf = fminf(fmaxf(ceilf((tb - t) * inv_dt), 1.0f), (float)jb);
-      uint32_t j = (uint32_t)kf;
-      while (j > 1u && !(fmaf((float)(j - 1u), dt, t) < tb)) --j;
-      while (j < jb && fmaf((float)j, dt, t) < tb) ++j;
+    const float d = t - bits_float((float_bits(t) & 0x7f800000u) + 0x00800000u);  // t - B, exact, < 0
+    // j: the first step at or past tb (lim if none), an estimate from the
+    // division corrected with compares; they are exact wherever
+    // t + j dt <= B, which the check below establishes for the final j
+    const float kf = fminf(fmaxf(ceilf((tb - t) * inv_dt), 1.0f), 4194304.0f);
+    uint32_t j = (uint32_t)kf < lim ? (uint32_t)kf : lim;
+    while (j > 1u && !(fmaf((float)(j - 1u), dt, t) < tb)) --j;
+    while (j < lim && fmaf((float)j, dt, t) < tb) ++j;
+    if (fmaf((float)j, dt, d) <= 0.0f) {  // sign of t + j dt - B, exact
       t = fmaf((float)j, dt, t);
       n += j;
       return k + j;
     }
+    // the run leaves the binade first: the most steps that stay at or below B
+    const float jf = fminf(fmaxf(floorf(-d * inv_dt), 0.0f), 4194304.0f);
+    uint32_t jb = (uint32_t)jf < lim ? (uint32_t)jf : lim;
+    while (jb > 0u && fmaf((float)jb, dt, d) > 0.0f) --jb;
+    while (jb < lim && fmaf((float)(jb + 1u), dt, d) <= 0.0f) ++jb;
     t = fmaf((float)jb, dt, t);
     n += jb;
     k += jb;
     if (jb == lim) break;
-    // the next step leaves the binade (t < tb, n < cap, k < max_steps still hold)
+    // the crossing step (t < tb, n < cap, k < max_steps still hold)
     t = t + dt;
     ++n;
     ++k;
