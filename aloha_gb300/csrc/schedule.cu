@@ -30,7 +30,7 @@ namespace {
 constexpr uint8_t kNoChunk = 0xff;
 constexpr float kProbeStride = 16.0f;  // samples per probe step
 constexpr int kProbeMaxSteps = 8192;   // per brick (the probe only estimates)
-constexpr int kSortThreads = 256;      // slots per histogram / scatter CTA
+constexpr int kSortThreads = 1024;     // slots per histogram / scatter CTA
 constexpr int kScanThreads = 1024;
 
 // Non-empty probe steps of one ray through every rank's bricks.
