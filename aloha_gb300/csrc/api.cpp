@@ -84,16 +84,20 @@ bool is_device_pointer(const void* p) {
   return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
 }
 
-// The device address of page-locked host memory registered with CUDA (e.g.
-// cudaHostAlloc / cudaMallocHost), or null for pageable memory.  Kernels on
-// GB300 write such memory directly over NVLink-C2C.
-void* pinned_device_alias(void* p) {
+// Where an output buffer lives, from one pointer query: device memory, or
+// host memory with the device address of page-locked memory registered with
+// CUDA (e.g. cudaHostAlloc / cudaMallocHost; null for pageable memory).
+// Kernels on GB300 write page-locked memory directly over NVLink-C2C.
+bool classify_output(void* p, void** pinned_alias) {
+  *pinned_alias = nullptr;
   cudaPointerAttributes attr;
   if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
     cudaGetLastError();
-    return nullptr;
+    return false;
   }
-  return attr.type == cudaMemoryTypeHost ? attr.devicePointer : nullptr;
+  if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) return true;
+  if (attr.type == cudaMemoryTypeHost) *pinned_alias = attr.devicePointer;
+  return false;
 }
 
 }  // namespace
@@ -123,6 +127,8 @@ struct aloha_ctx {
   int n_ranks = 0;
   std::vector<int> brick_rank;
   std::vector<KdNode> tree;
+  OrderCache order_cache;  // eye-independent part of the visibility orders
+  bool order_cache_valid = false;
   // views
   std::vector<ViewState> views;
   DeviceBuffer views_dev, sched_dev;
@@ -283,7 +289,11 @@ int prepare_view(aloha_ctx* c, int view, cudaStream_t s) {
     for (auto& vv : c->views) vv.dirty = true;
   }
   if (!v.dirty) return ALOHA_OK;
-  v.sched = make_schedule(c->boxes, c->brick_rank, c->n_ranks, c->tree, c->params.order_mode, v.org);
+  if (!c->order_cache_valid) {
+    c->order_cache = build_order_cache(c->boxes, c->brick_rank, c->n_ranks);
+    c->order_cache_valid = true;
+  }
+  v.sched = make_schedule(c->boxes, c->brick_rank, c->n_ranks, c->tree, c->params.order_mode, v.org, c->order_cache);
   // every rank appears exactly once in the composite order
   std::vector<char> seen(c->n_ranks, 0);
   std::vector<int> order;
@@ -386,7 +396,8 @@ bool use_rank_split(const aloha_ctx* c, const FrameArgs& f, const ViewState& v) 
 }
 
 int plan_chunk_order(aloha_ctx* c, const FrameArgs& f, int view, int cw, int ch, cudaStream_t s, const int** order,
-                     int* chunks, bool auto_order = true);
+                     int* chunks, bool auto_order = true, unsigned int* zero_work = nullptr,
+                     unsigned long long* zero_samples = nullptr);
 
 // Rank-split launch of a single view (mask, plan and render kernels).
 int launch_split(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
@@ -434,8 +445,9 @@ int launch_split(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
 // The cost-ordered chunk list of a single view when the chunk-order mode asks
 // for one (probe and sort kernels on `s`); *order stays null for ring order.
 // Automatic mode orders frames of 512^2 pixels or more when auto_order is set.
+// The probe also zeroes the given counters (only when *order is set).
 int plan_chunk_order(aloha_ctx* c, const FrameArgs& f, int view, int cw, int ch, cudaStream_t s, const int** order,
-                     int* chunks, bool auto_order) {
+                     int* chunks, bool auto_order, unsigned int* zero_work, unsigned long long* zero_samples) {
   const ViewState& v = c->views[view];
   *order = nullptr;
   const bool probed = c->chunk_order_mode == ALOHA_CHUNKS_PROBED ||
@@ -457,6 +469,8 @@ int plan_chunk_order(aloha_ctx* c, const FrameArgs& f, int view, int cw, int ch,
   o.cid = reinterpret_cast<int*>(w + key_words);
   o.hist = w + key_words + slots;
   o.order = reinterpret_cast<int*>(w + key_words + slots + hist);
+  o.zero_work = zero_work;
+  o.zero_samples = zero_samples;
   CUDA_TRY(c, launch_chunk_order(o, s));
   *order = o.order;
   *chunks = (int)n_chunks;
@@ -464,9 +478,14 @@ int plan_chunk_order(aloha_ctx* c, const FrameArgs& f, int view, int cw, int ch,
 }
 
 // One persistent render launch of a single view (resets the work counter).
+// Zeroes the sample counter f.counter and the work counter itself (in the
+// chunk probe when there is one).
 int launch_single(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   const ViewState& v = c->views[view];
-  if (use_rank_split(c, f, v)) return launch_split(c, f, view, s);
+  if (use_rank_split(c, f, v)) {
+    CUDA_TRY(c, cudaMemsetAsync(f.counter, 0, sizeof(unsigned long long), s));
+    return launch_split(c, f, view, s);
+  }
   if (c->split_mode == ALOHA_SPLIT_RANKS && f.fb && !f.rank_images && !f.rank_depth && c->n_ranks > 1) {
     if (c->n_ranks > kSplitMaxRanks)
       return c->fail(ALOHA_ERR_UNSUPPORTED, "rank split: %d ranks exceed %d", c->n_ranks, kSplitMaxRanks);
@@ -497,15 +516,17 @@ int launch_single(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   b.work_counter = static_cast<unsigned int*>(c->work.ptr);
   int chunks = 0;
   const int* order = nullptr;
-  int rc = plan_chunk_order(c, f, view, cw, ch, s, &order, &chunks);
+  int rc = plan_chunk_order(c, f, view, cw, ch, s, &order, &chunks, true, b.work_counter, f.counter);
   if (rc) return rc;
   if (order) {
     b.chunk_order = order;
     b.total_tiles = chunks;
+  } else {
+    CUDA_TRY(c, cudaMemsetAsync(c->work.ptr, 0, sizeof(unsigned int), s));
+    CUDA_TRY(c, cudaMemsetAsync(f.counter, 0, sizeof(unsigned long long), s));
   }
   const int warps_per_block = kRenderThreads / 32;
   const int grid = std::max(1, std::min(c->grid_blocks, (b.total_tiles + warps_per_block - 1) / warps_per_block));
-  CUDA_TRY(c, cudaMemsetAsync(c->work.ptr, 0, sizeof(unsigned int), s));
   CUDA_TRY(c, launch_render_warps(b, cw, ch, grid, false, s));
   return ALOHA_OK;
 }
@@ -561,6 +582,7 @@ int set_partition(aloha_ctx* c, int n_ranks) {
   c->n_ranks = n_ranks;
   c->brick_rank = br;
   c->tree = tree;
+  c->order_cache_valid = false;
   for (auto& v : c->views) v.dirty = true;
   invalidate_training(c);
   return ALOHA_OK;
@@ -869,6 +891,7 @@ int aloha_set_rank_assignment(aloha_ctx* c, const int* brick_rank, int n_bricks,
   c->n_ranks = n_ranks;
   c->brick_rank.assign(brick_rank, brick_rank + n_bricks);
   c->tree.clear();
+  c->order_cache_valid = false;
   for (auto& v : c->views) v.dirty = true;
   invalidate_training(c);
   return ALOHA_OK;
@@ -964,8 +987,8 @@ int aloha_render(aloha_ctx* c, int view, uint32_t* fb, void* stream) {
   const size_t npx = (size_t)v.width * v.height;
   // A pinned host frame buffer is written by the kernel directly; pageable
   // host memory goes through a device staging buffer.
-  const bool host = !is_device_pointer(fb);
-  void* pinned = host ? pinned_device_alias(fb) : nullptr;
+  void* pinned = nullptr;
+  const bool host = !classify_output(fb, &pinned);
   if (pinned) {
     a.fb = static_cast<uint32_t*>(pinned);
   } else if (host) {
@@ -974,7 +997,6 @@ int aloha_render(aloha_ctx* c, int view, uint32_t* fb, void* stream) {
   } else {
     a.fb = fb;
   }
-  CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
   rc = launch_single(c, a, view, s);
   if (rc) return rc;
   c->samples_valid = true;
@@ -1006,7 +1028,6 @@ int aloha_render_partials(aloha_ctx* c, int view, float* rank_images, float* ran
   a.rank_images = host_img ? reinterpret_cast<float4*>(stage) : reinterpret_cast<float4*>(rank_images);
   a.rank_depth = rank_depth ? (host_depth ? reinterpret_cast<float*>(stage + img_bytes) : rank_depth) : nullptr;
   a.fb = nullptr;
-  CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
   rc = launch_single(c, a, view, s);
   if (rc) return rc;
   c->samples_valid = true;

@@ -98,6 +98,9 @@ struct ChunkOrderArgs {
   int* cid;          // [n_slots] chunk id per slot
   uint32_t* hist;    // [kOrderClasses][chunk_order_blocks(n_slots)] counts, then offsets
   int* order;        // [chunks] chunk ids, most expensive first
+  // counters of the render launch that follows, zeroed by the probe (or null)
+  unsigned int* zero_work;
+  unsigned long long* zero_samples;
 };
 int chunk_order_blocks(int n_slots);
 cudaError_t launch_chunk_order(const ChunkOrderArgs& a, cudaStream_t s);

@@ -9,6 +9,8 @@
 
 #include <algorithm>
 #include <climits>
+#include <utility>
+#include <vector>
 
 namespace aloha {
 
@@ -114,23 +116,14 @@ std::vector<int> kd_order(const std::vector<KdNode>& tree, const float eye[3]) {
   return order;
 }
 
-std::vector<int> face_order(const std::vector<Box>& item_bounds, const std::vector<char>& item_has_boxes,
-                            const float eye[3]) {
-  const int n = (int)item_bounds.size();
-  std::vector<int> order;
-  std::vector<std::vector<int>> work;
-  std::vector<int> all(n);
-  for (int i = 0; i < n; ++i) all[i] = i;
-  work.push_back(all);
-  while (!work.empty()) {
-    std::vector<int> items = std::move(work.back());
-    work.pop_back();
-    if (items.size() <= 1) {
-      order.insert(order.end(), items.begin(), items.end());
-      continue;
-    }
-    bool split = false;
-    for (int a = 0; a < 3 && !split; ++a) {
+namespace {
+
+// Splits `items` recursively (first axis, then the lowest candidate plane that
+// separates them into two non-empty sides); returns the subtree's node.
+int build_face_node(FaceTree& t, const std::vector<Box>& item_bounds, const std::vector<char>& item_has_boxes,
+                    std::vector<int> items) {
+  if (items.size() > 1) {
+    for (int a = 0; a < 3; ++a) {
       std::vector<float> planes;
       for (int it : items)
         if (item_has_boxes[it]) {
@@ -153,66 +146,118 @@ std::vector<int> face_order(const std::vector<Box>& item_bounds, const std::vect
           }
         }
         if (!separates || below.empty() || above.empty()) continue;
-        // the eye's side comes first (pushed last)
-        if (eye[a] < p) {
-          work.push_back(std::move(above));
-          work.push_back(std::move(below));
-        } else {
-          work.push_back(std::move(below));
-          work.push_back(std::move(above));
-        }
-        split = true;
-        break;
+        const int id = (int)t.nodes.size();
+        t.nodes.push_back(FaceTree::Node{a, p, -1, -1});
+        const int lo = build_face_node(t, item_bounds, item_has_boxes, std::move(below));
+        const int hi = build_face_node(t, item_bounds, item_has_boxes, std::move(above));
+        t.nodes[id].first = lo;
+        t.nodes[id].second = hi;
+        return id;
       }
-    }
-    if (!split) {
-      std::vector<std::pair<float, int>> byd;
-      for (int it : items) {
-        float d2 = 0.f;
-        for (int a = 0; a < 3; ++a) {
-          const float c = item_has_boxes[it] ? (item_bounds[it].lo[a] + item_bounds[it].hi[a]) * 0.5f : eye[a];
-          d2 += (c - eye[a]) * (c - eye[a]);
-        }
-        byd.push_back({d2, it});
-      }
-      std::stable_sort(byd.begin(), byd.end(), [](const std::pair<float, int>& l, const std::pair<float, int>& r) {
-        return l.first < r.first;
-      });
-      for (auto& e : byd) order.push_back(e.second);
     }
   }
+  // one item, or no plane separates them: ordered by distance per view
+  const int id = (int)t.nodes.size();
+  t.nodes.push_back(FaceTree::Node{-1, 0.f, (int)t.items.size(), (int)(t.items.size() + items.size())});
+  t.items.insert(t.items.end(), items.begin(), items.end());
+  return id;
+}
+
+void visit_face_node(const FaceTree& t, int id, const std::vector<Box>& item_bounds,
+                     const std::vector<char>& item_has_boxes, const float eye[3], std::vector<int>& out) {
+  const FaceTree::Node& nd = t.nodes[id];
+  if (nd.axis >= 0) {
+    // the eye's side first
+    const bool below_first = eye[nd.axis] < nd.plane;
+    visit_face_node(t, below_first ? nd.first : nd.second, item_bounds, item_has_boxes, eye, out);
+    visit_face_node(t, below_first ? nd.second : nd.first, item_bounds, item_has_boxes, eye, out);
+    return;
+  }
+  if (nd.second - nd.first <= 1) {
+    out.insert(out.end(), t.items.begin() + nd.first, t.items.begin() + nd.second);
+    return;
+  }
+  std::vector<std::pair<float, int>> byd;
+  byd.reserve(nd.second - nd.first);
+  for (int k = nd.first; k < nd.second; ++k) {
+    const int it = t.items[k];
+    float d2 = 0.f;
+    for (int a = 0; a < 3; ++a) {
+      const float c = item_has_boxes[it] ? (item_bounds[it].lo[a] + item_bounds[it].hi[a]) * 0.5f : eye[a];
+      d2 += (c - eye[a]) * (c - eye[a]);
+    }
+    byd.push_back({d2, it});
+  }
+  std::stable_sort(byd.begin(), byd.end(), [](const std::pair<float, int>& l, const std::pair<float, int>& r) {
+    return l.first < r.first;
+  });
+  for (auto& e : byd) out.push_back(e.second);
+}
+
+}  // namespace
+
+FaceTree build_face_tree(const std::vector<Box>& item_bounds, const std::vector<char>& item_has_boxes) {
+  FaceTree t;
+  std::vector<int> all(item_bounds.size());
+  for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
+  if (!all.empty()) build_face_node(t, item_bounds, item_has_boxes, std::move(all));
+  return t;
+}
+
+void face_order(const FaceTree& t, const std::vector<Box>& item_bounds, const std::vector<char>& item_has_boxes,
+                const float eye[3], std::vector<int>& out) {
+  out.clear();
+  if (!t.nodes.empty()) visit_face_node(t, 0, item_bounds, item_has_boxes, eye, out);
+}
+
+std::vector<int> face_order(const std::vector<Box>& item_bounds, const std::vector<char>& item_has_boxes,
+                            const float eye[3]) {
+  std::vector<int> order;
+  face_order(build_face_tree(item_bounds, item_has_boxes), item_bounds, item_has_boxes, eye, order);
   return order;
 }
 
+OrderCache build_order_cache(const std::vector<Box>& bricks, const std::vector<int>& brick_rank, int n_ranks) {
+  OrderCache c;
+  const int nb = (int)bricks.size();
+  c.brick_has.assign(nb, 1);
+  c.bricks = build_face_tree(bricks, c.brick_has);
+  c.rank_bounds.assign(n_ranks, Box::empty());
+  c.rank_has.assign(n_ranks, 0);
+  for (int b = 0; b < nb; ++b) {
+    const int r = brick_rank[b];
+    if (r < 0 || r >= n_ranks) continue;
+    c.rank_has[r] = 1;
+    for (int a = 0; a < 3; ++a) {
+      c.rank_bounds[r].lo[a] = std::min(c.rank_bounds[r].lo[a], bricks[b].lo[a]);
+      c.rank_bounds[r].hi[a] = std::max(c.rank_bounds[r].hi[a], bricks[b].hi[a]);
+    }
+  }
+  c.ranks = build_face_tree(c.rank_bounds, c.rank_has);
+  return c;
+}
+
 Schedule make_schedule(const std::vector<Box>& bricks, const std::vector<int>& brick_rank, int n_ranks,
-                       const std::vector<KdNode>& tree, int order_mode, const float eye[3]) {
+                       const std::vector<KdNode>& tree, int order_mode, const float eye[3], const OrderCache& cache) {
   const int nb = (int)bricks.size();
   Schedule s;
   // brick order: every brick is its own item
-  std::vector<char> has(nb, 1);
-  std::vector<int> border = face_order(bricks, has, eye);
+  std::vector<int> border;
+  face_order(cache.bricks, bricks, cache.brick_has, eye, border);
   // rank order
-  if (order_mode == ALOHA_ORDER_REFERENCE_KD && !tree.empty()) {
+  if (order_mode == ALOHA_ORDER_REFERENCE_KD && !tree.empty())
     s.rank_order = kd_order(tree, eye);
-  } else {
-    std::vector<Box> rb(n_ranks, Box::empty());
-    std::vector<char> rhas(n_ranks, 0);
-    for (int b = 0; b < nb; ++b) {
-      const int r = brick_rank[b];
-      rhas[r] = 1;
-      for (int a = 0; a < 3; ++a) {
-        rb[r].lo[a] = std::min(rb[r].lo[a], bricks[b].lo[a]);
-        rb[r].hi[a] = std::max(rb[r].hi[a], bricks[b].hi[a]);
-      }
-    }
-    s.rank_order = face_order(rb, rhas, eye);
-  }
-  s.rank_start.assign(1, 0);
-  for (int r = 0; r < n_ranks; ++r) {
-    for (int b : border)
-      if (brick_rank[b] == r) s.rank_bricks.push_back(b);
-    s.rank_start.push_back((int)s.rank_bricks.size());
-  }
+  else
+    face_order(cache.ranks, cache.rank_bounds, cache.rank_has, eye, s.rank_order);
+  // each rank's bricks in brick order (CSR by rank id)
+  s.rank_start.assign(n_ranks + 1, 0);
+  for (int b = 0; b < nb; ++b)
+    if (brick_rank[b] >= 0 && brick_rank[b] < n_ranks) ++s.rank_start[brick_rank[b] + 1];
+  for (int r = 0; r < n_ranks; ++r) s.rank_start[r + 1] += s.rank_start[r];
+  s.rank_bricks.resize(s.rank_start[n_ranks]);
+  std::vector<int> fill(s.rank_start.begin(), s.rank_start.end() - 1);
+  for (int b : border)
+    if (brick_rank[b] >= 0 && brick_rank[b] < n_ranks) s.rank_bricks[fill[brick_rank[b]]++] = b;
   return s;
 }
 

@@ -80,6 +80,10 @@ __device__ __forceinline__ uint8_t cost_class(uint32_t c) {
 // Four threads per ring slot (lanes 4s..4s+3 of a warp): each probes one ray
 // of the chunk's 2x2 sample; the slot's class comes from the largest.
 __global__ void probe_chunks_kernel(ChunkOrderArgs a) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (a.zero_work) *a.zero_work = 0u;
+    if (a.zero_samples) *a.zero_samples = 0ull;
+  }
   const DevView& v = a.f.views[a.view];
   const int W = v.width, H = v.height, R = v.n_ranks;
   const int* __restrict__ order = a.f.sched + v.sched;
