@@ -148,9 +148,14 @@ def _stream(stream) -> int:
     return int(getattr(stream, "cuda_stream", 0))
 
 
+_F3 = ctypes.c_float * 3
+
+
 def _f3(v):
-    a = (ctypes.c_float * 3)(*[float(t) for t in v])
-    return a
+    try:
+        return _F3(*v)  # Python floats and ints convert directly
+    except TypeError:
+        return _F3(*[float(t) for t in v])
 
 
 def make_desc(d: dict) -> BrickDesc:
