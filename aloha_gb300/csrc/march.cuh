@@ -253,7 +253,8 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
         // colour unchanged, so only t and the sample count advance (the same
         // t += dt sequence as full samples) up to tb; the test resumes there.
         // The first is always taken.  With exact steps the rest of the run is
-        // a jump per binade crossed (and per checkpoint the hook needs).
+        // one jump (one more per power of two it crosses, and one per
+        // checkpoint the hook needs).
         if constexpr (!Hook::kActive) {
           ++n;
           t = t + dt;
