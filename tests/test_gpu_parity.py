@@ -48,6 +48,35 @@ def assert_same_fb(a, b):
         raise AssertionError(f"{len(diff)} pixels differ; first at ({x},{y}): {a[y, x]:08x} vs {b[y, x]:08x}")
 
 
+@pytest.mark.parametrize("split", SPLITS)
+def test_rank_assignment_changes(gpu_ctx_factory, oracle, split):
+    """The visibility orders are cached per brick set and rank assignment;
+    every change of either (partitionKD, an explicit assignment, back again)
+    must rebuild them.  The same views render after each change."""
+    vol, descs, vox, tf = T.chopsuey_scene(48, 8)
+    W, H = 64, 56
+    cams = T.cameras((48, 48, 48), 3, W, H, seed=27)
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=8)
+    ctx.set_render_split(split)
+    assignment = [0, 2, 1, 0, 2, 1, 1, 0]  # 3 virtual ranks of uneven brick sets
+    for step in ("kd8", "explicit3", "kd4"):
+        if step == "explicit3":
+            ctx.set_rank_assignment(assignment, 3)
+        elif step == "kd4":
+            ctx.set_ranks(4)
+        for cam in cams:
+            fb, samples = gpu_frame(ctx, cam, W, H)
+            if step == "kd8":
+                ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=8)
+            elif step == "explicit3":
+                ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H, oracle.make_params(), n_ranks=3,
+                                    brick_rank=assignment)
+            else:
+                ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=4)
+            assert_same_fb(fb, ref["fb"])
+            assert samples == ref["samples"]
+
+
 def test_plain_c1_bit_exact(gpu_ctx_factory, oracle):
     vol, descs, vox, tf = T.c1_scene()
     cam = S.axis_camera((64, 64, 64), 512, 512)
