@@ -118,96 +118,117 @@ std::vector<int> kd_order(const std::vector<KdNode>& tree, const float eye[3]) {
 
 namespace {
 
-// Splits `items` recursively (first axis, then the lowest candidate plane that
-// separates them into two non-empty sides); returns the subtree's node.
-int build_face_node(FaceTree& t, const std::vector<Box>& item_bounds, const std::vector<char>& item_has_boxes,
-                    std::vector<int> items) {
-  if (items.size() > 1) {
-    for (int a = 0; a < 3; ++a) {
-      std::vector<float> planes;
-      for (int it : items)
-        if (item_has_boxes[it]) {
-          planes.push_back(item_bounds[it].lo[a]);
-          planes.push_back(item_bounds[it].hi[a]);
+// The first axis-aligned plane (by axis, then position) that separates `items`
+// into two non-empty sides, or false.
+bool find_split(const std::vector<Box>& item_bounds, const std::vector<char>& item_has_boxes,
+                const std::vector<int>& items, int& axis, float& plane, std::vector<int>& below,
+                std::vector<int>& above) {
+  if (items.size() <= 1) return false;
+  for (int a = 0; a < 3; ++a) {
+    std::vector<float> planes;
+    for (int it : items)
+      if (item_has_boxes[it]) {
+        planes.push_back(item_bounds[it].lo[a]);
+        planes.push_back(item_bounds[it].hi[a]);
+      }
+    std::sort(planes.begin(), planes.end());
+    planes.erase(std::unique(planes.begin(), planes.end()), planes.end());
+    for (float p : planes) {
+      below.clear();
+      above.clear();
+      bool separates = true;
+      for (int it : items) {
+        if (!item_has_boxes[it] || item_bounds[it].hi[a] <= p)
+          below.push_back(it);
+        else if (item_bounds[it].lo[a] >= p)
+          above.push_back(it);
+        else {
+          separates = false;
+          break;
         }
-      std::sort(planes.begin(), planes.end());
-      planes.erase(std::unique(planes.begin(), planes.end()), planes.end());
-      for (float p : planes) {
-        std::vector<int> below, above;
-        bool separates = true;
-        for (int it : items) {
-          if (!item_has_boxes[it] || item_bounds[it].hi[a] <= p)
-            below.push_back(it);
-          else if (item_bounds[it].lo[a] >= p)
-            above.push_back(it);
-          else {
-            separates = false;
-            break;
-          }
-        }
-        if (!separates || below.empty() || above.empty()) continue;
-        const int id = (int)t.nodes.size();
-        t.nodes.push_back(FaceTree::Node{a, p, -1, -1});
-        const int lo = build_face_node(t, item_bounds, item_has_boxes, std::move(below));
-        const int hi = build_face_node(t, item_bounds, item_has_boxes, std::move(above));
-        t.nodes[id].first = lo;
-        t.nodes[id].second = hi;
-        return id;
+      }
+      if (separates && !below.empty() && !above.empty()) {
+        axis = a;
+        plane = p;
+        return true;
       }
     }
   }
-  // one item, or no plane separates them: ordered by distance per view
-  const int id = (int)t.nodes.size();
-  t.nodes.push_back(FaceTree::Node{-1, 0.f, (int)t.items.size(), (int)(t.items.size() + items.size())});
-  t.items.insert(t.items.end(), items.begin(), items.end());
-  return id;
-}
-
-void visit_face_node(const FaceTree& t, int id, const std::vector<Box>& item_bounds,
-                     const std::vector<char>& item_has_boxes, const float eye[3], std::vector<int>& out) {
-  const FaceTree::Node& nd = t.nodes[id];
-  if (nd.axis >= 0) {
-    // the eye's side first
-    const bool below_first = eye[nd.axis] < nd.plane;
-    visit_face_node(t, below_first ? nd.first : nd.second, item_bounds, item_has_boxes, eye, out);
-    visit_face_node(t, below_first ? nd.second : nd.first, item_bounds, item_has_boxes, eye, out);
-    return;
-  }
-  if (nd.second - nd.first <= 1) {
-    out.insert(out.end(), t.items.begin() + nd.first, t.items.begin() + nd.second);
-    return;
-  }
-  std::vector<std::pair<float, int>> byd;
-  byd.reserve(nd.second - nd.first);
-  for (int k = nd.first; k < nd.second; ++k) {
-    const int it = t.items[k];
-    float d2 = 0.f;
-    for (int a = 0; a < 3; ++a) {
-      const float c = item_has_boxes[it] ? (item_bounds[it].lo[a] + item_bounds[it].hi[a]) * 0.5f : eye[a];
-      d2 += (c - eye[a]) * (c - eye[a]);
-    }
-    byd.push_back({d2, it});
-  }
-  std::stable_sort(byd.begin(), byd.end(), [](const std::pair<float, int>& l, const std::pair<float, int>& r) {
-    return l.first < r.first;
-  });
-  for (auto& e : byd) out.push_back(e.second);
+  return false;
 }
 
 }  // namespace
 
+// Built with an explicit work list (a chain of bricks nests as deep as it is
+// long): each job is an item set and the parent slot its node fills.
 FaceTree build_face_tree(const std::vector<Box>& item_bounds, const std::vector<char>& item_has_boxes) {
   FaceTree t;
-  std::vector<int> all(item_bounds.size());
-  for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
-  if (!all.empty()) build_face_node(t, item_bounds, item_has_boxes, std::move(all));
+  struct Job {
+    std::vector<int> items;
+    int parent, side;  // side 0: the parent's `first` (below), 1: its `second` (above)
+  };
+  std::vector<Job> jobs;
+  {
+    std::vector<int> all(item_bounds.size());
+    for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
+    if (!all.empty()) jobs.push_back(Job{std::move(all), -1, 0});
+  }
+  std::vector<int> below, above;
+  while (!jobs.empty()) {
+    Job j = std::move(jobs.back());
+    jobs.pop_back();
+    const int id = (int)t.nodes.size();
+    if (j.parent >= 0) (j.side == 0 ? t.nodes[j.parent].first : t.nodes[j.parent].second) = id;
+    int axis = 0;
+    float plane = 0.f;
+    if (find_split(item_bounds, item_has_boxes, j.items, axis, plane, below, above)) {
+      t.nodes.push_back(FaceTree::Node{axis, plane, -1, -1});
+      jobs.push_back(Job{above, id, 1});
+      jobs.push_back(Job{below, id, 0});
+    } else {
+      // one item, or no plane separates them: ordered by distance per view
+      t.nodes.push_back(FaceTree::Node{-1, 0.f, (int)t.items.size(), (int)(t.items.size() + j.items.size())});
+      t.items.insert(t.items.end(), j.items.begin(), j.items.end());
+    }
+  }
   return t;
 }
 
 void face_order(const FaceTree& t, const std::vector<Box>& item_bounds, const std::vector<char>& item_has_boxes,
                 const float eye[3], std::vector<int>& out) {
   out.clear();
-  if (!t.nodes.empty()) visit_face_node(t, 0, item_bounds, item_has_boxes, eye, out);
+  if (t.nodes.empty()) return;
+  std::vector<int> stack(1, 0);
+  std::vector<std::pair<float, int>> byd;
+  while (!stack.empty()) {
+    const FaceTree::Node& nd = t.nodes[stack.back()];
+    stack.pop_back();
+    if (nd.axis >= 0) {
+      // the eye's side first (pushed last)
+      const bool below_first = eye[nd.axis] < nd.plane;
+      stack.push_back(below_first ? nd.second : nd.first);
+      stack.push_back(below_first ? nd.first : nd.second);
+      continue;
+    }
+    if (nd.second - nd.first <= 1) {
+      out.insert(out.end(), t.items.begin() + nd.first, t.items.begin() + nd.second);
+      continue;
+    }
+    byd.clear();
+    for (int k = nd.first; k < nd.second; ++k) {
+      const int it = t.items[k];
+      float d2 = 0.f;
+      for (int a = 0; a < 3; ++a) {
+        const float c = item_has_boxes[it] ? (item_bounds[it].lo[a] + item_bounds[it].hi[a]) * 0.5f : eye[a];
+        d2 += (c - eye[a]) * (c - eye[a]);
+      }
+      byd.push_back({d2, it});
+    }
+    std::stable_sort(byd.begin(), byd.end(), [](const std::pair<float, int>& l, const std::pair<float, int>& r) {
+      return l.first < r.first;
+    });
+    for (auto& e : byd) out.push_back(e.second);
+  }
 }
 
 std::vector<int> face_order(const std::vector<Box>& item_bounds, const std::vector<char>& item_has_boxes,
