@@ -147,6 +147,7 @@ struct aloha_ctx {
   int split_mode = ALOHA_SPLIT_AUTO;
   DeviceBuffer split_images, split_masks, split_items, split_done;
   int split_grid_n_tf = -1, split_grid_blocks = 0;
+  bool split_grid_many = false;
   uint64_t last_samples = 0;
   bool samples_valid = false;
 
@@ -432,13 +433,15 @@ int launch_split(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   if (c->split_done.bytes != before) CUDA_TRY(c, cudaMemsetAsync(c->split_done.ptr, 0, c->split_done.bytes, s));
   a.chunk_done = static_cast<unsigned int*>(c->split_done.ptr);
   a.work_counter = static_cast<unsigned int*>(c->work.ptr);
-  if (c->split_grid_n_tf != c->n_tf) {
-    const int per_sm = render_split_blocks_per_sm(c->n_tf);
+  const bool many = R >= kAutoRankSplitRanks;
+  if (c->split_grid_n_tf != c->n_tf || c->split_grid_many != many) {
+    const int per_sm = render_split_blocks_per_sm(c->n_tf, many);
     if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "render occupancy query failed");
     c->split_grid_blocks = per_sm * c->num_sms;
     c->split_grid_n_tf = c->n_tf;
+    c->split_grid_many = many;
   }
-  CUDA_TRY(c, launch_render_split(a, c->split_grid_blocks, s));
+  CUDA_TRY(c, launch_render_split(a, c->split_grid_blocks, many, s));
   return ALOHA_OK;
 }
 

@@ -163,7 +163,9 @@ inline int macrocells(const DevBrick& b) {
 }
 // CTAs of the render kernel that fit on one SM for a chunk shape (0 if the shape is unknown).
 int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf, bool batch);
-cudaError_t launch_render_split(const SplitArgs& a, int grid, cudaStream_t s);
-int render_split_blocks_per_sm(int n_tf);
+// `many_ranks` selects the instance tuned for many short (chunk, rank) items.
+constexpr int kManyRankSplitBlocks = 7;  // CTAs per SM
+cudaError_t launch_render_split(const SplitArgs& a, int grid, bool many_ranks, cudaStream_t s);
+int render_split_blocks_per_sm(int n_tf, bool many_ranks);
 
 }  // namespace aloha
