@@ -147,6 +147,7 @@ struct aloha_ctx {
   int split_mode = ALOHA_SPLIT_AUTO;
   DeviceBuffer split_images, split_masks, split_items, split_done;
   int split_grid_n_tf = -1, split_grid_blocks = 0;
+  int chunk_order_slots = -1;  // slot count of the chunk-order buffer's current layout
   bool split_grid_many = false;
   uint64_t last_samples = 0;
   bool samples_valid = false;
@@ -466,12 +467,20 @@ int plan_chunk_order(aloha_ctx* c, const FrameArgs& f, int view, int cw, int ch,
   const size_t n_chunks = (size_t)((v.width + cw - 1) / cw) * ((v.height + ch - 1) / ch);
   const size_t slots = (size_t)o.n_slots, hist = (size_t)kOrderClasses * chunk_order_blocks(o.n_slots);
   const size_t key_words = (slots + 3) / 4;  // uint8 keys, padded to whole words
+  const size_t before = c->chunk_order.bytes;
   CUDA_TRY(c, c->chunk_order.ensure((key_words + slots + hist + n_chunks) * sizeof(uint32_t)));
   uint32_t* w = static_cast<uint32_t*>(c->chunk_order.ptr);
   o.key = reinterpret_cast<uint8_t*>(w);
   o.cid = reinterpret_cast<int*>(w + key_words);
   o.hist = w + key_words + slots;
   o.order = reinterpret_cast<int*>(w + key_words + slots + hist);
+  o.n_chunks = (int)n_chunks;
+  // the histogram is zero between launches of one layout (the scatter clears
+  // it); a new buffer or another slot count puts it elsewhere
+  if (c->chunk_order.bytes != before || c->chunk_order_slots != o.n_slots) {
+    CUDA_TRY(c, cudaMemsetAsync(o.hist, 0, hist * sizeof(uint32_t), s));
+    c->chunk_order_slots = o.n_slots;
+  }
   o.zero_work = zero_work;
   o.zero_samples = zero_samples;
   CUDA_TRY(c, launch_chunk_order(o, s));

@@ -96,8 +96,9 @@ struct ChunkOrderArgs {
   int n_slots;       // ring slots of the chunk grid (the probe's input order)
   uint8_t* key;      // [n_slots] cost class per slot (0xff off the grid)
   int* cid;          // [n_slots] chunk id per slot
-  uint32_t* hist;    // [kOrderClasses][chunk_order_blocks(n_slots)] counts, then offsets
+  uint32_t* hist;    // [kOrderClasses][chunk_order_blocks(n_slots)] counts, then offsets; zero between launches
   int* order;        // [chunks] chunk ids, most expensive first
+  int n_chunks;      // chunks of the grid (entries of `order`)
   // counters of the render launch that follows, zeroed by the probe (or null)
   unsigned int* zero_work;
   unsigned long long* zero_samples;

@@ -15,8 +15,9 @@
 // class keeps neighbouring chunks together.  The order only changes when a
 // pixel is rendered, never how, so frames are bit-identical to ring order.
 //
-// Kernels: probe (4 threads per ring slot), per-CTA class histogram, one-CTA
-// exclusive scan of the histogram table (class-major), stable scatter.
+// Kernels: probe (4 threads per ring slot; each CTA also adds its class
+// counts into its sort block's histogram column), one-CTA exclusive scan of
+// the histogram table (class-major), stable scatter (which zeroes the table).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -30,7 +31,8 @@ namespace {
 constexpr uint8_t kNoChunk = 0xff;
 constexpr float kProbeStride = 16.0f;  // samples per probe step
 constexpr int kProbeMaxSteps = 8192;   // per brick (the probe only estimates)
-constexpr int kSortThreads = 1024;     // slots per histogram / scatter CTA
+constexpr int kSortThreads = 1024;     // slots per sort block (histogram column, scatter CTA)
+constexpr int kProbeThreads = 256;     // 4 per slot: 64 slots per probe CTA
 constexpr int kScanThreads = 1024;
 
 // Non-empty probe steps of one ray through every rank's bricks.
@@ -78,12 +80,17 @@ __device__ __forceinline__ uint8_t cost_class(uint32_t c) {
 }
 
 // Four threads per ring slot (lanes 4s..4s+3 of a warp): each probes one ray
-// of the chunk's 2x2 sample; the slot's class comes from the largest.
+// of the chunk's 2x2 sample; the slot's class comes from the largest.  A CTA
+// covers kProbeThreads / 4 slots and adds its class counts into the histogram
+// column of the sort block (kSortThreads slots) it belongs to.
 __global__ void probe_chunks_kernel(ChunkOrderArgs a) {
+  __shared__ uint32_t h[kOrderClasses];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     if (a.zero_work) *a.zero_work = 0u;
     if (a.zero_samples) *a.zero_samples = 0ull;
   }
+  for (int i = threadIdx.x; i < kOrderClasses; i += kProbeThreads) h[i] = 0;
+  __syncthreads();
   const DevView& v = a.f.views[a.view];
   const int W = v.width, H = v.height, R = v.n_ranks;
   const int* __restrict__ order = a.f.sched + v.sched;
@@ -102,24 +109,16 @@ __global__ void probe_chunks_kernel(ChunkOrderArgs a) {
   c = max(c, __shfl_xor_sync(0xffffffffu, c, 1));
   c = max(c, __shfl_xor_sync(0xffffffffu, c, 2));
   if (q == 0 && slot < a.n_slots) {
-    a.key[slot] = valid ? cost_class(c) : kNoChunk;
+    const uint8_t k = valid ? cost_class(c) : kNoChunk;
+    a.key[slot] = k;
     a.cid[slot] = cx + cxn * cy;
-  }
-}
-
-// Per-CTA counts of each class over kSortThreads consecutive slots, stored
-// class-major: hist[class * n_blocks + block].
-__global__ void __launch_bounds__(kSortThreads) class_hist_kernel(ChunkOrderArgs a) {
-  __shared__ uint32_t h[kOrderClasses];
-  for (int i = threadIdx.x; i < kOrderClasses; i += kSortThreads) h[i] = 0;
-  __syncthreads();
-  const int slot = blockIdx.x * kSortThreads + threadIdx.x;
-  if (slot < a.n_slots) {
-    const uint8_t k = a.key[slot];
-    if (k != kNoChunk) atomicAdd(&h[k], 1u);
+    if (valid) atomicAdd(&h[k], 1u);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < kOrderClasses; i += kSortThreads) a.hist[i * gridDim.x + blockIdx.x] = h[i];
+  const int blocks = (a.n_slots + kSortThreads - 1) / kSortThreads;
+  const int block = (int)(((long long)blockIdx.x * (kProbeThreads / 4)) / kSortThreads);
+  for (int i = threadIdx.x; i < kOrderClasses; i += kProbeThreads)
+    if (h[i]) atomicAdd(a.hist + i * blocks + block, h[i]);
 }
 
 // Exclusive scan of the histogram table in place (one CTA; each thread scans
@@ -172,24 +171,33 @@ __global__ void __launch_bounds__(kSortThreads) class_scatter_kernel(ChunkOrderA
   const unsigned rank = __popc(peers & ((1u << lane) - 1u));
   if (k != kNoChunk && lane == __ffs(peers) - 1) wc[w][k] = __popc(peers);
   __syncthreads();
-  if (k == kNoChunk) return;
-  uint32_t pos = a.hist[k * gridDim.x + blockIdx.x] + rank;
-  for (int e = 0; e < w; ++e) pos += wc[e][k];
-  a.order[pos] = a.cid[slot];
+  if (k != kNoChunk) {
+    uint32_t pos = a.hist[k * gridDim.x + blockIdx.x] + rank;
+    for (int e = 0; e < w; ++e) pos += wc[e][k];
+    if (pos < (uint32_t)a.n_chunks) a.order[pos] = a.cid[slot];
+  }
+  // the block's histogram column is consumed: zero it for the next launch
+  __syncthreads();
+  for (int i = threadIdx.x; i < kOrderClasses; i += kSortThreads) a.hist[i * gridDim.x + blockIdx.x] = 0u;
 }
 
 }  // namespace
 
 int chunk_order_blocks(int n_slots) { return (n_slots + kSortThreads - 1) / kSortThreads; }
 
+// The histogram (a.hist, kOrderClasses x chunk_order_blocks(n_slots)) must be
+// zero when this is called; the scatter leaves it zero again.
 cudaError_t launch_chunk_order(const ChunkOrderArgs& a, cudaStream_t s) {
-  const int probe_grid = (int)(((long long)a.n_slots * 4 + 255) / 256);
-  probe_chunks_kernel<<<probe_grid, 256, 0, s>>>(a);
+  static_assert(kSortThreads % (kProbeThreads / 4) == 0, "probe CTAs must tile sort blocks");
+  const int probe_grid = (int)(((long long)a.n_slots * 4 + kProbeThreads - 1) / kProbeThreads);
+  probe_chunks_kernel<<<probe_grid, kProbeThreads, 0, s>>>(a);
   const int blocks = chunk_order_blocks(a.n_slots);
-  class_hist_kernel<<<blocks, kSortThreads, 0, s>>>(a);
   class_scan_kernel<<<1, kScanThreads, 0, s>>>(a, kOrderClasses * blocks);
   class_scatter_kernel<<<blocks, kSortThreads, 0, s>>>(a);
-  return cudaGetLastError();
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)  // counts may stay behind: clear them for the next launch
+    cudaMemsetAsync(a.hist, 0, (size_t)kOrderClasses * blocks * sizeof(uint32_t), s);
+  return e;
 }
 
 }  // namespace aloha

@@ -359,11 +359,11 @@ def main():
     ctx.set_render_tile(tw, th)
     ctx.set_chunk_order(chunks)
     kernel = "render_split_kernel" if split == abi.SPLIT_RANKS else f"render_warps_kernel<{tw},{th}>"
-    # our kernels per frame: the render, plus the chunk probe and the class
-    # histogram, scan and scatter of the cost order, and for the rank split
-    # its mask, three scan kernels and emit
+    # our kernels per frame: the render, plus the chunk probe (which also
+    # counts the classes), scan and scatter of the cost order, and for the
+    # rank split its mask, three scan kernels and emit
     probed = chunks == abi.CHUNKS_PROBED or (chunks == abi.CHUNKS_AUTO and W * H >= 512 * 512)
-    launches_per_frame = (6 if split == abi.SPLIT_RANKS else 1) + (4 if probed else 0)
+    launches_per_frame = (6 if split == abi.SPLIT_RANKS else 1) + (3 if probed else 0)
 
     steps = [mine[k % len(mine)] for k in range(args.steps)]
     for k in range(args.warmup):
