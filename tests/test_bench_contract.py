@@ -10,6 +10,8 @@ import os
 import subprocess
 import sys
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ARGS = ["--impl", "reference", "--n", "64", "--size", "64", "--cameras", "4", "--steps", "3", "--warmup", "3"]
 
@@ -46,3 +48,33 @@ def test_reference_arm_other_ranks_print_nothing():
     out = _run({"RANK": "1", "WORLD_SIZE": "2"})
     assert out.returncode == 0, out.stderr[-2000:]
     assert out.stdout.strip() == ""
+
+
+@pytest.mark.gpu
+def test_gpu_arm_prints_the_contract_line():
+    """The GPU arm at a small size: value, e2e with the copied bytes, the
+    roofline of the dominant kernel, the CPU baseline, clocks and the count of
+    this library's kernel launches."""
+    pytest.importorskip("torch")
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    args = ["--n", "128", "--size", "256", "--cameras", "8", "--steps", "4", "--warmup", "3", "--no-adjoint",
+            "--no-large", "--no-batched", "--cpu-seconds", "1"]
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py")] + args, capture_output=True, text=True,
+                         timeout=900, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    d = json.loads([ln for ln in out.stdout.splitlines() if ln.strip()][-1])
+    assert d["unit"] == "Gsamples/s" and d["value"] > 0 and d["steps"] == 4 and d["warmup"] == 3
+    assert d["gpu_launches"] >= d["steps"]
+    e2e = d["e2e"]
+    assert e2e["value"] > 0 and e2e["h2d_bytes_per_step"] > 0 and e2e["d2h_bytes_per_step"] == 256 * 256 * 4
+    r = d["roofline"]
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s" and r["achieved"] > 0 and r["peak"] > 0
+    assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-9
+    cb = d["cpu_baseline"]
+    assert cb["value"] > 0 and cb["cores"] >= 1 and cb["kind"] == "port"
+    clk = d["clocks"]
+    assert {"sm_mhz", "sm_max_mhz", "samples", "reasons"} <= set(clk)
+    assert not {"hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown"} & set(clk["reasons"])
+
