@@ -1,8 +1,8 @@
 """Ray-tile autotuner for the batched render with a JSON cache.
 
-The persistent batched kernel comes in three ray-tile shapes (8x8, 16x8 and
-32x4 pixels per CTA); ``aloha_batch_autotune`` times each on the batch itself
-with CUDA events and keeps the fastest.  This module caches that choice per
+The persistent batched kernel comes in four ray-tile shapes (8x4, 8x8, 16x8
+and 32x4 pixels per warp chunk); ``aloha_batch_autotune`` times each on the
+batch itself with CUDA events and keeps the fastest.  This module caches that choice per
 (GPU, batch configuration) in a JSON file so later processes skip the sweep.
 """
 from __future__ import annotations
