@@ -220,8 +220,8 @@ int aloha_get_stats(aloha_ctx* ctx, aloha_stats* out);
 typedef struct aloha_batch aloha_batch;
 
 int aloha_batch_create(aloha_ctx* ctx, const int* views, int n_items, uint32_t* const* fbs, aloha_batch** out);
-/* Ray-tile shape of the persistent kernel: 8x8, 16x8 or 32x4 pixels per CTA;
- * ctas_per_sm = 0 picks the occupancy limit. */
+/* Ray-tile shape of the persistent kernel: 8x4, 8x8, 16x8 or 32x4 pixels per
+ * warp chunk; ctas_per_sm = 0 picks the occupancy limit. */
 int aloha_batch_set_config(aloha_batch* b, int tile_w, int tile_h, int ctas_per_sm);
 int aloha_batch_get_config(const aloha_batch* b, int* tile_w, int* tile_h, int* ctas_per_sm);
 int aloha_batch_launch(aloha_batch* b, void* stream);
