@@ -1,6 +1,6 @@
 // Property check of the host visibility orders (aloha_gb300/csrc/order.cpp):
 // on random grids of bricks (uneven cuts, some cells missing) and random eye
-// points, with a random rank assignment,
+// points, with a random rank assignment (some leaving ranks without bricks),
 //  * the brick order lists every brick once, and every pair is listed in an
 //    order that some separating plane justifies (the first brick on the
 //    eye's side of it, or the eye in the gap);
@@ -80,9 +80,14 @@ int main() {
     const int R = 1 + (int)(U(rng) * nb);
     std::vector<int> br(nb);
     for (int b = 0; b < nb; ++b) br[b] = b < R ? b : (int)(U(rng) * R);
+    if (it % 4 == 3 && R > 1)  // an explicit assignment may leave ranks without bricks
+      for (int b = 0; b < nb; ++b) br[b] = (int)(U(rng) * (R / 2 + 1)) * 2 % R;
     const aloha::OrderCache cache = aloha::build_order_cache(boxes, br, R);
     // ranks' boxes are pairwise separable only when each rank holds one brick
-    const bool ranks_are_bricks = R == nb;
+    std::vector<int> per_rank(R, 0);
+    for (int b = 0; b < nb; ++b) ++per_rank[br[b]];
+    bool ranks_are_bricks = R == nb;
+    for (int r = 0; r < R; ++r) ranks_are_bricks = ranks_are_bricks && per_rank[r] == 1;
     for (int e = 0; e < 12; ++e) {
       float eye[3];
       for (int a = 0; a < 3; ++a) eye[a] = (U(rng) * 3.f - 1.f) * cuts[a].back();
