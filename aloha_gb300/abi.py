@@ -290,9 +290,10 @@ class Context:
 
     def backward(self, view: int, dl_drgba, dl_dtf, dl_ddensity, grid_lo, grid_dims, stream=None):
         """Accumulate dL/dtf and dL/ddensity (on the grid at grid_lo, dims x,y,z) for dL/dRGBA.
-        dl_dtf may be None: density gradient only (the replay then skips empty space)."""
-        lo = np.ascontiguousarray(grid_lo, dtype=np.int32)
-        dims = np.ascontiguousarray(grid_dims, dtype=np.int32)
+        dl_dtf may be None: density gradient only (the replay then skips empty space).
+        dl_ddensity may be None: transfer-function gradient only (grid_lo, grid_dims ignored)."""
+        lo = None if grid_lo is None else np.ascontiguousarray(grid_lo, dtype=np.int32)
+        dims = None if grid_dims is None else np.ascontiguousarray(grid_dims, dtype=np.int32)
         self._check(self._lib.aloha_backward(self.h, view, _addr(dl_drgba), _addr(dl_dtf), _addr(dl_ddensity),
                                              _addr(lo), _addr(dims), _stream(stream)))
 

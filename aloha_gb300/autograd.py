@@ -9,10 +9,34 @@ csrc/adjoint.cu) and accumulates the gradients.
 """
 from __future__ import annotations
 
+import weakref
+
 import torch
 
 from . import abi
 from . import volfile
+
+
+class DensityTracker:
+    """Whether a density tensor still holds what was last uploaded: the same
+    tensor object (held by a weak reference, so a new tensor that reuses a
+    freed block at the same address never passes) at the same autograd
+    version counter (bumped by every in-place update)."""
+
+    def __init__(self):
+        self._ref = None
+        self._version = None
+
+    def current(self, t: torch.Tensor) -> bool:
+        ref = self._ref() if self._ref is not None else None
+        return ref is t and t._version == self._version
+
+    def record(self, t: torch.Tensor):
+        self._ref = weakref.ref(t)
+        self._version = t._version
+
+    def invalidate(self):
+        self._ref = None
 
 
 class DifferentiableRenderer:
@@ -29,17 +53,31 @@ class DifferentiableRenderer:
         self.ctx = abi.Context(device)
         self._uploaded = False
         self._params = params
+        self._density = DensityTracker()
+        self.brick_uploads = 0  # bricks copied to the context so far
+
+    def invalidate(self):
+        """Forget the uploaded density: the next render uploads it again.  Needed
+        only after writes that bypass the tensor's version counter (through
+        ``tensor.data`` or another tensor sharing its storage)."""
+        self._density.invalidate()
 
     def _upload(self, tf: torch.Tensor, density: torch.Tensor):
-        vox = [volfile.brick_voxels(density.detach(), d) for d in self.descs]
-        if not self._uploaded:
-            self.ctx.set_bricks(self.descs, vox)
-            self.ctx.set_ranks(1)
-            self.ctx.set_params(**self._params)
-            self._uploaded = True
-        else:
-            for i, v in enumerate(vox):
-                self.ctx.update_brick(i, v)
+        if not self._density.current(density):
+            # the bricks (padding, macrocell tables) are rebuilt only when the
+            # density may have changed: another tensor object, or an in-place
+            # update of this one (which bumps its version counter)
+            vox = [volfile.brick_voxels(density.detach(), d) for d in self.descs]
+            if not self._uploaded:
+                self.ctx.set_bricks(self.descs, vox)
+                self.ctx.set_ranks(1)
+                self.ctx.set_params(**self._params)
+                self._uploaded = True
+            else:
+                for i, v in enumerate(vox):
+                    self.ctx.update_brick(i, v)
+            self.brick_uploads += len(vox)
+            self._density.record(density)
         self.ctx.set_transfer_function(tf.detach().contiguous())
 
     def set_camera(self, view: int, cam, width: int, height: int):
@@ -70,15 +108,19 @@ class _Render(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad):
         r: DifferentiableRenderer = ctx.renderer
+        want_tf, want_density = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        if not (want_tf or want_density):
+            return None, None, None, None, None
         grad = grad.contiguous().float()
-        # without a transfer-function gradient the backward skips empty space
-        dtf = torch.zeros(ctx.tf_shape, dtype=torch.float32, device=grad.device) \
-            if ctx.needs_input_grad[0] else None
-        dden = torch.zeros(ctx.density_shape, dtype=torch.float32, device=grad.device)
+        # without a transfer-function gradient the backward skips empty space;
+        # without a density gradient it skips the shading and stencil adjoints
+        dtf = torch.zeros(ctx.tf_shape, dtype=torch.float32, device=grad.device) if want_tf else None
+        dden = torch.zeros(ctx.density_shape, dtype=torch.float32, device=grad.device) if want_density else None
         stream = torch.cuda.current_stream()
         nz, ny, nx = ctx.density_shape
+        lo, dims = ((0, 0, 0), (nx, ny, nz)) if want_density else (None, None)
         for i, v in enumerate(ctx.views):
-            r.ctx.backward(v, grad[i], dtf, dden, (0, 0, 0), (nx, ny, nz), stream)
+            r.ctx.backward(v, grad[i], dtf, dden, lo, dims, stream)
         return dtf, dden, None, None, None
 
 

@@ -364,11 +364,13 @@ __device__ __forceinline__ void flush_tf(float* dtf_s, int n, int i, float pend[
 
 constexpr unsigned kBackwardGrab = 256;  // most items a backward warp takes per grab (8 rows of 32)
 
-// WITH_TF: also the transfer-function gradient.  Without it (density only)
+// WITH_TF: the transfer-function gradient; WITH_DENSITY: the density
+// gradient (at least one of them).  Without the transfer-function gradient
 // the replay skips empty macrocells like the forward: a sample there has
 // transfer-function alpha 0 at both lookup entries, so its density and
 // shading gradients vanish and only the alpha entries would receive any.
-template <bool WITH_TF>
+// Without the density gradient the shading and stencil adjoints are skipped.
+template <bool WITH_TF, bool WITH_DENSITY>
 __global__ void __launch_bounds__(128, 5) backward_kernel(TrainArgs a, int view) {
   extern __shared__ float4 smem[];
   float4* tf_s = smem;                                         // n_tf + 4 entries
@@ -449,17 +451,19 @@ __global__ void __launch_bounds__(128, 5) backward_kernel(TrainArgs a, int view)
             }
             const float kc = oma * c.w * shade;
             const float dch[4] = {g.x * kc, g.y * kc, g.z * kc, dA};
+            if (WITH_TF) {
+  #pragma unroll
+              for (int ch = 0; ch < 4; ++ch) {
+                pend[ch] = fmaf(1.f - wt, dch[ch], pend[ch]);
+                pend[4 + ch] = fmaf(wt, dch[ch], pend[4 + ch]);
+              }
+            }
+            if (!WITH_DENSITY) return;
             const float ds = oma * c.w * gc;
             const float de[4] = {e1.x - e0.x, e1.y - e0.y, e1.z - e0.z, e1.w - e0.w};
             float dv = 0.f;
   #pragma unroll
-            for (int ch = 0; ch < 4; ++ch) {
-              if (WITH_TF) {
-                pend[ch] = fmaf(1.f - wt, dch[ch], pend[ch]);
-                pend[4 + ch] = fmaf(wt, dch[ch], pend[4 + ch]);
-              }
-              dv = fmaf(dch[ch], de[ch], dv);
-            }
+            for (int ch = 0; ch < 4; ++ch) dv = fmaf(dch[ch], de[ch], dv);
             dv *= nf;
             // shading backward: s = .1 + .9 |q|, q = (g.d)/|g + 1e-4|
             const float ex = s.gx + 1e-4f, ey = s.gy + 1e-4f, ez = s.gz + 1e-4f;
@@ -508,9 +512,11 @@ int forward_train_blocks_per_sm(int n_tf) {
 }
 
 cudaError_t launch_backward(const TrainArgs& a, int view, int grid, cudaStream_t s) {
-  const bool with_tf = a.dtf != nullptr;
+  const bool with_tf = a.dtf != nullptr, with_density = a.dgrid4 != nullptr;
+  if (!with_tf && !with_density) return cudaErrorInvalidValue;
   const size_t smem = backward_smem(a.n_tf, with_tf);
-  void (*k)(TrainArgs, int) = with_tf ? backward_kernel<true> : backward_kernel<false>;
+  void (*k)(TrainArgs, int) = !with_tf ? backward_kernel<false, true>
+                                       : (with_density ? backward_kernel<true, true> : backward_kernel<true, false>);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -532,13 +538,13 @@ int backward_blocks_per_sm(int n_tf) {
   // the instance with the transfer-function gradient needs more shared memory
   const size_t smem = backward_smem(n_tf, true);
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(backward_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaFuncSetAttribute(backward_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, backward_kernel<true>, 128, smem) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, backward_kernel<true, true>, 128, smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }

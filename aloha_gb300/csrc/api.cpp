@@ -631,6 +631,15 @@ void ctx_frame_args(aloha_ctx* c, FrameArgs* a) { *a = frame_args(c); }
 int ctx_prepare_view(aloha_ctx* c, int view, cudaStream_t s) { return prepare_view(c, view, s); }
 void ctx_mark_samples(aloha_ctx* c) { c->samples_valid = true; }
 bool ctx_is_device_pointer(const void* p) { return is_device_pointer(p); }
+bool device_pointer_on(const void* p, int device) {
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (attr.type == cudaMemoryTypeManaged) return true;
+  return attr.type == cudaMemoryTypeDevice && attr.device == device;
+}
 
 }  // namespace aloha
 
@@ -1250,7 +1259,9 @@ int aloha_forward(aloha_ctx* c, int view, float* rgba, int checkpoint_every, voi
 
 int aloha_backward(aloha_ctx* c, int view, const float* dl_drgba, float* dl_dtf, float* dl_ddensity,
                    const int* grid_lo, const int* grid_dims, void* stream) {
-  if (!c || !dl_drgba || !dl_ddensity || !grid_lo || !grid_dims) return ALOHA_ERR_NULL_POINTER;
+  if (!c || !dl_drgba) return ALOHA_ERR_NULL_POINTER;
+  if (!dl_dtf && !dl_ddensity) return c->fail(ALOHA_ERR_NULL_POINTER, "neither dl_dtf nor dl_ddensity given");
+  if (dl_ddensity && (!grid_lo || !grid_dims)) return c->fail(ALOHA_ERR_NULL_POINTER, "dl_ddensity needs its grid");
   if (view < 0 || view >= (int)c->views.size()) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "view %d", view);
   int rc = check_trainable(c);
   if (rc) return rc;
@@ -1258,11 +1269,15 @@ int aloha_backward(aloha_ctx* c, int view, const float* dl_drgba, float* dl_dtf,
   TrainState& t = v.train;
   if (!t.valid)
     return c->fail(ALOHA_ERR_NOT_READY, "view %d has no forward checkpoints for the current scene and camera", view);
-  for (int a = 0; a < 3; ++a)
-    if (grid_dims[a] < 1) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "grid dims must be positive");
-  const size_t grid_elems = (size_t)grid_dims[0] * grid_dims[1] * grid_dims[2];
-  std::vector<int4> origin(c->descs.size());
-  for (size_t b = 0; b < c->descs.size(); ++b) {
+  const bool with_density = dl_ddensity != nullptr;
+  size_t grid_elems = 0;
+  std::vector<int4> origin(with_density ? c->descs.size() : 0);
+  if (with_density) {
+    for (int a = 0; a < 3; ++a)
+      if (grid_dims[a] < 1) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "grid dims must be positive");
+    grid_elems = (size_t)grid_dims[0] * grid_dims[1] * grid_dims[2];
+  }
+  for (size_t b = 0; b < origin.size(); ++b) {
     const aloha_brick_desc& d = c->descs[b];
     for (int a = 0; a < 3; ++a)
       if (d.voxel_lo[a] < grid_lo[a] || d.voxel_hi[a] > grid_lo[a] + grid_dims[a])
@@ -1277,7 +1292,7 @@ int aloha_backward(aloha_ctx* c, int view, const float* dl_drgba, float* dl_dtf,
   if (overflow) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "a ray needed more checkpoints than reserved");
   const size_t npx = t.npx, tf_bytes = (size_t)c->n_tf * 4 * sizeof(float), g_bytes = grid_elems * sizeof(float);
   const bool h_dl = !is_device_pointer(dl_drgba), h_tf = dl_dtf && !is_device_pointer(dl_dtf),
-             h_grid = !is_device_pointer(dl_ddensity);
+             h_grid = with_density && !is_device_pointer(dl_ddensity);
   // device staging for host arguments, in one block: dL/dRGBA, dL/dtf, dL/ddensity, origins
   const size_t off_tf = h_dl ? npx * sizeof(float4) : 0;
   const size_t off_grid = off_tf + (h_tf ? tf_bytes : 0);
@@ -1289,21 +1304,24 @@ int aloha_backward(aloha_ctx* c, int view, const float* dl_drgba, float* dl_dtf,
   a.dtf = h_tf ? reinterpret_cast<float*>(st + off_tf) : dl_dtf;
   float* grid_out = h_grid ? reinterpret_cast<float*>(st + off_grid) : dl_ddensity;
   a.brick_grid_origin = reinterpret_cast<const int4*>(st + off_org);
-  for (int k = 0; k < 3; ++k) a.grid_dims[k] = grid_dims[k];
-  // the kernel accumulates into x-quads (vector atomics), folded into the grid afterwards
-  CUDA_TRY(c, c->grad4.ensure(grid_elems * sizeof(float4)));
-  a.dgrid4 = static_cast<float4*>(c->grad4.ptr);
-  CUDA_TRY(c, cudaMemsetAsync(a.dgrid4, 0, grid_elems * sizeof(float4), s));
+  if (with_density) {
+    for (int k = 0; k < 3; ++k) a.grid_dims[k] = grid_dims[k];
+    // the kernel accumulates into x-quads (vector atomics), folded into the grid afterwards
+    CUDA_TRY(c, c->grad4.ensure(grid_elems * sizeof(float4)));
+    a.dgrid4 = static_cast<float4*>(c->grad4.ptr);
+    CUDA_TRY(c, cudaMemsetAsync(a.dgrid4, 0, grid_elems * sizeof(float4), s));
+  }
   if (h_dl) CUDA_TRY(c, cudaMemcpyAsync(st, dl_drgba, npx * sizeof(float4), cudaMemcpyHostToDevice, s));
   if (h_tf) CUDA_TRY(c, cudaMemcpyAsync(a.dtf, dl_dtf, tf_bytes, cudaMemcpyHostToDevice, s));
   if (h_grid) CUDA_TRY(c, cudaMemcpyAsync(grid_out, dl_ddensity, g_bytes, cudaMemcpyHostToDevice, s));
-  CUDA_TRY(c, cudaMemcpyAsync(st + off_org, origin.data(), origin.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  if (with_density)
+    CUDA_TRY(c, cudaMemcpyAsync(st + off_org, origin.data(), origin.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
   const int per_sm = backward_blocks_per_sm(c->n_tf);
   if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "backward occupancy query failed");
   CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
   CUDA_TRY(c, cudaMemsetAsync(a.work_count + 2, 0, sizeof(unsigned), s));  // the backward's grab counter
   CUDA_TRY(c, launch_backward(a, view, c->num_sms * per_sm, s));
-  CUDA_TRY(c, launch_fold_quads(a.dgrid4, grid_out, grid_dims, s));
+  if (with_density) CUDA_TRY(c, launch_fold_quads(a.dgrid4, grid_out, grid_dims, s));
   c->samples_valid = true;
   if (h_tf) CUDA_TRY(c, cudaMemcpyAsync(dl_dtf, a.dtf, tf_bytes, cudaMemcpyDeviceToHost, s));
   if (h_grid) CUDA_TRY(c, cudaMemcpyAsync(dl_ddensity, grid_out, g_bytes, cudaMemcpyDeviceToHost, s));

@@ -5,9 +5,8 @@
 // allocates per call (cudaMalloc / cudaFree).  Some callers cannot allocate
 // device memory at that point: a compositing stage called from inside
 // another library's frame loop whose memory pool forbids extra allocations,
-// real-time hosts that ban allocation after start-up, or code that must not
-// synchronize the device (cudaFree does).  This entry point stages the order
-// in a fixed device array that lives in the library instead:
+// or a real-time host that bans allocation after start-up.  This entry point
+// stages the order in a fixed device array that lives in the library instead:
 //
 //   * the array is a file-scope __device__ array of kNoAllocMaxRanks ints
 //     (16 KB); every GPU that loads the library holds it until exit;
@@ -20,13 +19,19 @@
 //   * more than kNoAllocMaxRanks ranks is rejected with
 //     ALOHA_ERR_OUT_OF_RANGE.
 //
-// Images and the frame buffer must be device memory (the caller owns them);
-// the order is read from host memory.
+// Images and the frame buffer must be device memory of the current device
+// (the caller owns them); the order is read from host memory.  The call
+// takes a private snapshot of the order, checks the snapshot and copies the
+// snapshot into the array, so the caller may change or free its order buffer
+// as soon as the call returns.  The snapshot lives in pageable memory: the
+// runtime stages it before the copy call returns, after waiting for the
+// stream's earlier work, so the call is not fully asynchronous.
 #include <cuda_runtime.h>
 
 #include <cstring>
 #include <mutex>
 
+#include "batch_internal.h"
 #include "internal.h"
 
 namespace aloha {
@@ -58,15 +63,6 @@ cudaError_t order_scratch(int** out) {
   return cudaSuccess;
 }
 
-bool on_device(const void* p) {
-  cudaPointerAttributes attr;
-  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
-}
-
 }  // namespace
 }  // namespace aloha
 
@@ -78,13 +74,21 @@ extern "C" int aloha_composite_over_noalloc(const float* rank_images, const int*
     return ALOHA_ERR_INVALID_ARGUMENT;
   if (n_ranks > kNoAllocMaxRanks) return ALOHA_ERR_OUT_OF_RANGE;
   if (mode != ALOHA_COMPOSITE_FP32 && mode != ALOHA_COMPOSITE_UBYTE) return ALOHA_ERR_INVALID_ARGUMENT;
-  if (!on_device(rank_images) || !on_device(fb) || on_device(order)) return ALOHA_ERR_INVALID_ARGUMENT;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return ALOHA_ERR_CUDA;
+  if (!device_pointer_on(rank_images, dev) || !device_pointer_on(fb, dev) || ctx_is_device_pointer(order))
+    return ALOHA_ERR_INVALID_ARGUMENT;
+  // Snapshot first, then check and copy the snapshot: the caller's buffer is
+  // read once, here, so later changes to it cannot reach the kernel.
+  int snapshot[kNoAllocMaxRanks];
+  std::memcpy(snapshot, order, sizeof(int) * (size_t)n_ranks);
   for (int k = 0; k < n_ranks; ++k)
-    if (order[k] < 0 || order[k] >= n_ranks) return ALOHA_ERR_OUT_OF_RANGE;
+    if (snapshot[k] < 0 || snapshot[k] >= n_ranks) return ALOHA_ERR_OUT_OF_RANGE;
   int* d_order = nullptr;
   if (order_scratch(&d_order) != cudaSuccess) return ALOHA_ERR_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (cudaMemcpyAsync(d_order, order, sizeof(int) * (size_t)n_ranks, cudaMemcpyHostToDevice, s) != cudaSuccess)
+  // pageable source: staged by the runtime before the call returns
+  if (cudaMemcpyAsync(d_order, snapshot, sizeof(int) * (size_t)n_ranks, cudaMemcpyHostToDevice, s) != cudaSuccess)
     return ALOHA_ERR_CUDA;
   if (launch_composite_f32(reinterpret_cast<const float4*>(rank_images), d_order, n_ranks, width * height, mode, fb,
                            s) != cudaSuccess)

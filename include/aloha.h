@@ -202,9 +202,13 @@ int aloha_composite_over_rgba8(const uint32_t* rank_fbs, const int* order, int n
  * in a 16 KB device array compiled into the library (held by every GPU that
  * loads it until exit), whose address is looked up on the first call made on
  * each device, so that first call should come before any stream capture.
- * rank_images and fb must be device memory, order host memory; at most 4096
- * ranks (else ALOHA_ERR_OUT_OF_RANGE).  Calls share the staging array, so
- * calls that overlap on the GPU race: use one stream or wait in between. */
+ * rank_images and fb must be device memory of the current device, order host
+ * memory; at most 4096 ranks (else ALOHA_ERR_OUT_OF_RANGE).  The call reads
+ * `order` once into a private host snapshot, checks it and copies the
+ * snapshot, so the caller may change or free its buffer as soon as the call
+ * returns; that copy is from pageable memory, so the call first waits for the
+ * stream's earlier work.  Calls share the staging array, so calls that
+ * overlap on the GPU race: use one stream or wait in between. */
 int aloha_composite_over_noalloc(const float* rank_images, const int* order, int n_ranks, int width, int height,
                                  int mode, uint32_t* fb, void* stream);
 
@@ -253,7 +257,10 @@ int aloha_forward(aloha_ctx* ctx, int view, float* rgba, int checkpoint_every, v
  * clamped edge taps add into the voxel they copy.  Host or device buffers.
  * dl_dtf may be NULL: only the density gradient is computed, and the replay
  * then skips empty macrocells (their samples have transfer-function alpha 0,
- * so they contribute to the alpha entries of dl_dtf only). */
+ * so they contribute to the alpha entries of dl_dtf only).  dl_ddensity may
+ * be NULL (grid_lo and grid_dims are then ignored): only the transfer-function
+ * gradient is computed, without the shading and stencil adjoints.  At least
+ * one of the two must be given (else ALOHA_ERR_NULL_POINTER). */
 int aloha_backward(aloha_ctx* ctx, int view, const float* dl_drgba, float* dl_dtf, float* dl_ddensity,
                    const int* grid_lo, const int* grid_dims, void* stream);
 

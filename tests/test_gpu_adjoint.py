@@ -269,3 +269,76 @@ def test_backward_errors(gpu_ctx_factory):
     with pytest.raises(abi.AlohaError) as e:
         ctx.backward(0, img, dtf, dden, (0, 0, 0), (32, 32, 32))  # camera changed since the forward
     assert e.value.code == abi.ERR_NOT_READY
+
+
+@pytest.mark.parametrize("bricks", [1, 8])
+def test_tf_only_backward(gpu_ctx_factory, oracle, bricks):
+    """Without a density gradient (dl_ddensity NULL) the backward skips the
+    shading and stencil adjoints; its transfer-function gradient must match the
+    FP64 oracle and the full backward's (up to the order of the atomic adds)."""
+    n = 48
+    vol, descs, vox = density_scene(n, seed=13, bricks=bricks)
+    tf = S.ramp_tf()
+    W, H = 80, 72
+    ctx = setup(gpu_ctx_factory, descs, vox, tf)
+    rng = np.random.default_rng(61 + bricks)
+    full_tf = np.zeros((tf.shape[0], 4), np.float32)
+    full_den = np.zeros((n, n, n), np.float32)
+    only_tf = np.zeros((tf.shape[0], 4), np.float32)
+    ref_tf = np.zeros((tf.shape[0], 4))
+    for v, cam in enumerate(T.cameras((n, n, n), 2, W, H, seed=19)):
+        ctx.set_camera(v, *cam)
+        ctx.resize(v, W, H)
+        ctx.forward(v, np.zeros((H, W, 4), np.float32), 32)
+        dl = rng.uniform(-1, 1, (H, W, 4)).astype(np.float32)
+        ctx.backward(v, dl, full_tf, full_den, (0, 0, 0), (n, n, n))
+        ctx.backward(v, dl, only_tf, None, None, None)
+        ref_tf += oracle.adjoint(descs, vox, tf, oracle.make_camera(*cam), W, H, dl, (0, 0, 0), (n, n, n))["dtf"]
+    assert np.count_nonzero(only_tf) > 100
+    assert rel_err(only_tf, ref_tf) < 1e-3
+    np.testing.assert_allclose(only_tf, full_tf, rtol=1e-4, atol=1e-6 * float(np.abs(full_tf).max()))
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.backward(0, dl, None, None, None, None)
+    assert e.value.code == abi.ERR_NULL_POINTER
+
+
+def test_autograd_gradient_flags_and_uploads(gpu_ctx_factory):
+    """The binding computes only the gradients autograd asks for, and uploads
+    the bricks again only when the density tensor changed."""
+    torch = pytest.importorskip("torch")
+    from aloha_gb300.autograd import DifferentiableRenderer, render_views
+    n, W = 32, 40
+    vol = S.blob_field((n, n, n), 8, (2.0, 5.0), seed=27)
+    r = DifferentiableRenderer((n, n, n), bricks=1, checkpoint_every=16)
+    for v, cam in enumerate(T.cameras((n, n, n), 2, W, W, seed=29)):
+        r.set_camera(v, cam, W, W)
+    tf = torch.from_numpy(S.ramp_tf()).cuda()
+    target = torch.rand((2, W, W, 4), device="cuda")
+    den = torch.from_numpy(vol).cuda()
+    # both gradients: the reference for the transfer-function gradient below
+    tf_a = tf.clone().requires_grad_(True)
+    den_a = den.clone().requires_grad_(True)
+    ((render_views(r, tf_a, den_a, [0, 1], (W, W)) - target) ** 2).sum().backward()
+    uploads = r.brick_uploads
+    # transfer function only: no density gradient, and the same density
+    # tensor is not uploaded again
+    tf_b = tf.clone().requires_grad_(True)
+    ((render_views(r, tf_b, den_a.detach(), [0, 1], (W, W)) - target) ** 2).sum().backward()
+    assert r.brick_uploads == uploads + 1  # detach() is a new tensor object
+    uploads = r.brick_uploads
+    tf_c = tf.clone().requires_grad_(True)
+    den_c = den.clone()  # does not require grad
+    ((render_views(r, tf_c, den_c, [0, 1], (W, W)) - target) ** 2).sum().backward()
+    assert r.brick_uploads == uploads + 1
+    ((render_views(r, tf.clone().requires_grad_(True), den_c, [0, 1], (W, W)) - target) ** 2).sum().backward()
+    assert r.brick_uploads == uploads + 1  # unchanged density: no upload
+    den_c.mul_(1.0)  # in place: version bump, uploaded again
+    render_views(r, tf, den_c, [0, 1], (W, W))
+    assert r.brick_uploads == uploads + 2
+    torch.testing.assert_close(tf_c.grad, tf_a.grad, rtol=1e-4, atol=1e-6 * float(tf_a.grad.abs().max()))
+    torch.testing.assert_close(tf_b.grad, tf_a.grad, rtol=1e-4, atol=1e-6 * float(tf_a.grad.abs().max()))
+    # density only
+    den_d = den.clone().requires_grad_(True)
+    ((render_views(r, tf, den_d, [0, 1], (W, W)) - target) ** 2).sum().backward()
+    torch.testing.assert_close(den_d.grad, den_a.grad, rtol=1e-4, atol=1e-6 * float(den_a.grad.abs().max()))
+    r.close()

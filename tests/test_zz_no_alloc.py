@@ -42,6 +42,29 @@ def test_noalloc_composite_matches_allocating_composite(mode):
         assert torch.equal(got, want)
 
 
+def test_noalloc_composite_reads_the_order_once():
+    """A page-locked order buffer overwritten with out-of-range indices right
+    after the call returns must not reach the kernel: the call works on its own
+    snapshot of the order."""
+    torch = pytest.importorskip("torch")
+    from aloha_gb300 import abi
+    L = abi.lib()
+    stream = torch.cuda.current_stream()
+    n_ranks, H, W = 6, 64, 80
+    imgs = _images(torch, n_ranks, H, W, 5)
+    order_np = np.random.default_rng(5).permutation(n_ranks).astype(np.int32)
+    pinned = torch.from_numpy(order_np.copy()).pin_memory()
+    want = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+    got = torch.full((H, W), -1, dtype=torch.int32, device="cuda")
+    assert L.aloha_composite_over(imgs.data_ptr(), order_np.ctypes.data, n_ranks, W, H, 0, want.data_ptr(),
+                                  stream.cuda_stream) == abi.OK
+    assert L.aloha_composite_over_noalloc(imgs.data_ptr(), pinned.data_ptr(), n_ranks, W, H, 0, got.data_ptr(),
+                                          stream.cuda_stream) == abi.OK
+    pinned.fill_(1 << 20)  # out of range for every rank image
+    torch.cuda.synchronize()
+    assert torch.equal(got, want)
+
+
 def test_noalloc_composite_rejects_what_it_cannot_serve():
     torch = pytest.importorskip("torch")
     from aloha_gb300 import abi
