@@ -92,11 +92,8 @@ def quantize_u8(field: np.ndarray) -> np.ndarray:
 
 def normalize_raw(raw: np.ndarray) -> np.ndarray:
     """Volume::get's conversion (volume.h:75-88): uint8 /255, uint16 /65535, float as is."""
-    if raw.dtype == np.uint8:
-        return raw.astype(np.float32) / np.float32(255.0)
-    if raw.dtype == np.uint16:
-        return raw.astype(np.float32) / np.float32(65535.0)
-    return raw.astype(np.float32)
+    from .volfile import normalize_raw as _normalize
+    return _normalize(raw)
 
 
 def plain_c1_volume(seed: int = 1):

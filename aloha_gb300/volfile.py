@@ -13,6 +13,12 @@ all little-endian:
                interval<float> valueRange; float voxels[voxelRange volume]
 (box3i = 6 int32, box3f = 6 float32, x-fastest voxels).  The root voxel range
 is written as [0, dims+1) exactly as chopSuey does (chopSuey.cpp:251).
+
+Raw volumes (volume.h:37-98, FileMapping.cpp): a headerless x-fastest file of
+dims x*y*z voxels of 1, 2 or 4 bytes (uint8, uint16, float32), mapped into
+memory and read brick by brick; ``normalize_raw`` converts like Volume::get.
+``chop_raw`` is the chopSuey tool's volume path (chopSuey.cpp:361-441):
+raw file -> split -> .vol, one brick in memory at a time.
 """
 from __future__ import annotations
 
@@ -78,10 +84,15 @@ def grid_split(dims, cuts) -> list[dict]:
 
 
 def brick_voxels(volume, desc):
-    """The brick's voxel range of a (nz, ny, nx) volume (numpy or torch), contiguous."""
+    """The brick's voxel range of a (nz, ny, nx) volume (numpy or torch),
+    contiguous; numpy float volumes become float32, other numpy types keep
+    their type (a raw volume before normalisation)."""
     lo, hi = desc["voxel_lo"], desc["voxel_hi"]
     v = volume[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]]
-    return v.contiguous() if hasattr(v, "contiguous") else np.ascontiguousarray(v, dtype=np.float32)
+    if hasattr(v, "contiguous"):
+        return v.contiguous()
+    v = np.asarray(v)
+    return np.ascontiguousarray(v, dtype=np.float32 if v.dtype.kind == "f" else v.dtype)
 
 
 def write_vol(path: str, dims, descs, voxels) -> None:
@@ -123,3 +134,54 @@ def read_vol(path: str, bricks=None):
                 f.seek(4 * count, 1)
                 vox.append(None)
     return header, descs, vox
+
+
+RAW_TYPES = {"uint8": np.dtype("u1"), "uint16": np.dtype("<u2"), "float": np.dtype("<f4")}
+BPC_TYPES = {1: "uint8", 2: "uint16", 4: "float"}
+
+
+def normalize_raw(raw) -> np.ndarray:
+    """Volume::get's conversion (volume.h:75-88): uint8 /255, uint16 /65535,
+    float32 as is, each voxel converted to float and divided in float."""
+    raw = np.asarray(raw)
+    if raw.dtype == np.uint8:
+        return raw.astype(np.float32) / np.float32(255.0)
+    if raw.dtype == np.uint16:
+        return raw.astype(np.float32) / np.float32(65535.0)
+    return raw.astype(np.float32)
+
+
+def read_raw(path: str, dims, type_name: str) -> np.ndarray:
+    """Memory-maps a raw volume as a (z, y, x) array of its stored type; the
+    file must hold at least dims x*y*z voxels."""
+    if type_name not in RAW_TYPES:
+        raise ValueError(f"unknown voxel type {type_name!r} (uint8, uint16 or float)")
+    nx, ny, nz = (int(d) for d in dims)
+    if min(nx, ny, nz) <= 0:
+        raise ValueError("volume dimensions must be positive")
+    dt = RAW_TYPES[type_name]
+    import os
+    need = nx * ny * nz * dt.itemsize
+    have = os.path.getsize(path)
+    if have < need:
+        raise ValueError(f"{path}: {have} bytes, dims {nx}x{ny}x{nz} of {type_name} need {need}")
+    return np.memmap(path, dtype=dt, mode="r", shape=(nz, ny, nx))
+
+
+def chop_raw(raw_path: str, dims, type_name: str, n: int, out_path: str) -> list[dict]:
+    """chopSuey's volume path: split the raw volume into `n` bricks (at least
+    two, as the tool gives) and write them as a .vol file, each brick
+    normalised like Volume::get with its value range.  Returns the bricks."""
+    raw = read_raw(raw_path, dims, type_name)
+    descs = chopsuey_split(dims, n)
+    dims = [int(d) for d in dims]
+    with open(out_path, "wb") as f:
+        f.write(HEADER.pack(len(descs), 0, 0, 0, *dims, 0, 0, 0, *[d + 1 for d in dims],
+                            0.0, 0.0, 0.0, *[float(d) for d in dims]))
+        for d in descs:
+            v = np.ascontiguousarray(normalize_raw(brick_voxels(raw, d)), dtype="<f4")
+            d["value_range"] = [float(v.min()), float(v.max())]
+            f.write(BRICK.pack(*d["cell_lo"], *d["cell_hi"], *d["voxel_lo"], *d["voxel_hi"],
+                               *d["space_lo"], *d["space_hi"], *d["value_range"]))
+            f.write(v.tobytes())
+    return descs

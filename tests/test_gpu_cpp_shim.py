@@ -43,3 +43,38 @@ def test_cpp_renderer_matches_oracle(render_vol, oracle, tmp_path, n_ranks):
     ranks = n_ranks or 8
     ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H, oracle.make_params(), n_ranks=ranks)
     np.testing.assert_array_equal(fb, ref["fb"])
+
+
+def test_raw_volume_through_chopsuey_and_cpp_renderer(render_vol, oracle, tmp_path):
+    """A raw uint8 volume -> the chopSuey tool -> .vol -> the C++ renderer:
+    the frame equals the in-memory path (the same volume normalised and split
+    in Python, rendered through the C ABI) and the oracle."""
+    from aloha_gb300 import abi
+    from aloha_gb300 import chopsuey
+    from aloha_gb300 import scenes as S
+    raw = S.plain_c1_volume(seed=3)[:, :, :60]  # 60 x 64 x 64, x fastest
+    raw = np.ascontiguousarray(raw)
+    dims = (raw.shape[2], raw.shape[1], raw.shape[0])
+    raw_path, vpath, tpath, opath = (str(tmp_path / f) for f in ("in.raw", "s.vol", "tf.f32", "fb.u32"))
+    raw.tofile(raw_path)
+    assert chopsuey.main([raw_path, "-dims", *map(str, dims), "-type", "uint8", "-n", "6", "-o", vpath]) == 0
+    tf = S.ramp_tf()
+    tf.astype(np.float32).tofile(tpath)
+    W, H = 72, 64
+    cam = T.cameras(dims, 1, W, H, seed=43)[0]
+    args = [render_vol, vpath, tpath, str(tf.shape[0]), opath, str(W), str(H), "0"]
+    args += [repr(float(v)) for c in cam for v in c]
+    subprocess.run(args, check=True)
+    fb = np.fromfile(opath, dtype=np.uint32).reshape(H, W)
+    vol = V.normalize_raw(raw)
+    descs = V.chopsuey_split(dims, 6)
+    vox = [V.brick_voxels(vol, d) for d in descs]
+    with abi.Context(0) as ctx:
+        ctx.set_bricks(descs, vox)
+        ctx.set_transfer_function(tf)
+        ctx.set_params()
+        ctx.set_camera(0, *cam)
+        ctx.resize(0, W, H)
+        np.testing.assert_array_equal(ctx.render(0, width=W, height=H), fb)
+    ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H, oracle.make_params(), n_ranks=len(descs))
+    np.testing.assert_array_equal(fb, ref["fb"])
