@@ -50,11 +50,14 @@ __device__ __forceinline__ const int* rank_bricks(const TrainArgs& a, const DevV
 // see march_brick) are counted and stepped over without a `visit` (in one
 // jump when the steps are exact).  Only the density gradient may skip them: a
 // zero-alpha sample still carries a gradient for the alpha entries.
-template <bool SKIP, class Visit>
+//
+// With CAN_STOP the walk also ends, before the next sample, once *stop is set
+// (by the visitor).
+template <bool SKIP, bool CAN_STOP = false, class Visit>
 __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevView& v, const float4* tf_s,
                                                  const Ray& ray, uint32_t pixel, Walk w, float t_resume,
                                                  uint32_t nb0, bool resume, float4& color, uint32_t max_samples,
-                                                 Visit visit) {
+                                                 Visit visit, const bool* stop = nullptr) {
   const int* __restrict__ rb = rank_bricks(a, v);
   const int j1 = __ldg(a.sched + v.sched + 2);
   const float nf = (float)a.n_tf;
@@ -90,6 +93,7 @@ __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevVi
     float t_cell = t0;  // samples before it lie in a macrocell found non-empty
     while (t < t1 && color.w < a.et_alpha && nb < cap) {
       if (n == max_samples) return n;
+      if (CAN_STOP && *stop) return n;
       const float ux = fmaf(t, ray.d[0], ray.o[0]) - b.lo[0];
       const float uy = fmaf(t, ray.d[1], ray.o[1]) - b.lo[1];
       const float uz = fmaf(t, ray.d[2], ray.o[2]) - b.lo[2];
@@ -362,6 +366,61 @@ __device__ __forceinline__ void flush_tf(float* dtf_s, int n, int i, float pend[
   for (int k = 0; k < 8; ++k) pend[k] = 0.f;
 }
 
+// Near-opaque samples.  The closed form for the adjoint of the accumulated
+// alpha after sample i,
+//     gA = (g_a (1 - a_N) - g_rgb . (rgb_N - rgb_{i+1})) / (1 - a_{i+1}),
+// divides two vanishing quantities once a sample leaves almost no
+// transmittance, and gives 0 for a sample of alpha exactly 1 (1 - a = 0),
+// where the true value is g_a R_a - g_rgb . R_rgb with R the composite of the
+// rest of the ray normalised to the transmittance after the sample:
+//     R_a = prod_j (1 - alpha_j),  R_rgb = sum_j prod_{l<j} (1 - alpha_l) alpha_j s_j c_j.
+// The replay records such a sample as an event (the closed form stands in
+// for it meanwhile); after the segment, suffix_composite marches on from the
+// sample after it and the event's alpha adjoint is corrected by the
+// difference.  A ray has at most three events: each one cuts the
+// transmittance by more than 256 from above kVisible.
+constexpr float kOpaqueStep = 1.0f / 256.0f;  // alpha above 1 - 1/256
+constexpr float kVisible = 1e-5f;             // ... and the sample not hidden already
+constexpr int kMaxEvents = 3;
+
+struct OpaqueEvent {
+  Walk w;          // walk position of the sample (next jitter draw)
+  float t_next;    // t and brick sample count of the sample after it
+  uint32_t nb_next;
+  float4 after;    // colour after the sample
+  float oma;       // transmittance before it
+  float gA;        // the closed form's value
+  float value;     // interpolated value (transfer-function lookup)
+  float ux, uy, uz;
+  int brick;
+};
+
+// R after an event: the forward's following samples replayed from
+// (w, t_next, nb_next) with the colour after the event (so that early
+// termination ends the ray where the forward ended it), until R's
+// transmittance is below 2^-24 (the rest cannot move the result) or the ray
+// ends.  Skipped samples (alpha 0) leave R unchanged, so empty space is
+// stepped over.  Returns (R_rgb, R_a).
+__device__ __forceinline__ float4 suffix_composite(const TrainArgs& a, const DevView& v, const float4* tf_s,
+                                                   const Ray& ray, uint32_t pixel, const OpaqueEvent& e) {
+  float r0 = 0.f, r1 = 0.f, r2 = 0.f, tp = 1.0f;
+  bool stop = false;
+  float4 col = e.after;
+  walk_samples<true, true>(
+      a, v, tf_s, ray, pixel, e.w, e.t_next, e.nb_next, true, col, 0xffffffffu,
+      [&](const DevBrick&, float, const Walk&, uint32_t, float, float, float, const StencilOut&, float shade,
+          const float4& c, const float4&) {
+        const float k = tp * c.w * shade;
+        r0 = fmaf(k, c.x, r0);
+        r1 = fmaf(k, c.y, r1);
+        r2 = fmaf(k, c.z, r2);
+        tp = tp * (1.0f - c.w);
+        if (tp < 5.96e-8f) stop = true;
+      },
+      &stop);
+  return make_float4(r0, r1, r2, tp);
+}
+
 constexpr unsigned kBackwardGrab = 256;  // most items a backward warp takes per grab (8 rows of 32)
 
 // WITH_TF: the transfer-function gradient; WITH_DENSITY: the density
@@ -414,18 +473,37 @@ __global__ void __launch_bounds__(128, 5) backward_kernel(TrainArgs a, int view)
       // index is summed in registers and added to shared memory once per index
       int pend_i = INT_MIN;
       float pend[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      OpaqueEvent events[kMaxEvents];
+      int n_events = 0;
       nsamp += walk_samples<!WITH_TF>(
           a, v, tf_s, ray, pixel, w0, ck.t, ck.nb, true, color, a.k,
-          [&](const DevBrick& b, float, const Walk& wcur, uint32_t, float ux, float uy, float uz, const StencilOut& s,
-              float shade, const float4& c, const float4& col) {
+          [&](const DevBrick& b, float t, const Walk& wcur, uint32_t nb, float ux, float uy, float uz,
+              const StencilOut& s, float shade, const float4& c, const float4& col) {
             // Backward-only arithmetic below is free to contract and to use
             // approximate reciprocals (the gradient tolerance is relative); the
             // replay that feeds it is the exact forward.
             float4 nxt = col;  // state after this sample
             composite_step(nxt, c, shade);
-            const float tn = fmaxf(1.0f - nxt.w, 1e-6f);
-            const float gA = __fdividef(gfin - fmaf(g.x, F.x - nxt.x, fmaf(g.y, F.y - nxt.y, g.z * (F.z - nxt.z))), tn);
             const float oma = 1.0f - col.w;
+            const float tn1 = 1.0f - nxt.w;
+            // dL/d(accumulated alpha after this sample), closed form
+            const float gA =
+                __fdividef(gfin - fmaf(g.x, F.x - nxt.x, fmaf(g.y, F.y - nxt.y, g.z * (F.z - nxt.z))),
+                           fmaxf(tn1, 1e-6f));
+            if (tn1 < kOpaqueStep * oma && oma > kVisible && n_events < kMaxEvents) {
+              OpaqueEvent& e = events[n_events++];
+              e.w = wcur;
+              e.t_next = t + a.dt;
+              e.nb_next = nb + 1;
+              e.after = nxt;
+              e.oma = oma;
+              e.gA = gA;
+              e.value = s.value;
+              e.ux = ux;
+              e.uy = uy;
+              e.uz = uz;
+              e.brick = __ldg(rb + wcur.j);
+            }
             const float gc = fmaf(g.x, c.x, fmaf(g.y, c.y, g.z * c.z));
             const float dA = oma * fmaf(shade, gc, gA);  // dL/d(alpha of this sample)
             // transfer function lookup backward (the lookup of tf_lookup)
@@ -477,6 +555,30 @@ __global__ void __launch_bounds__(128, 5) backward_kernel(TrainArgs a, int view)
                              fmaf(ki, ray.d[1], -kc3 * ey), fmaf(ki, ray.d[2], -kc3 * ez));
           });
       if (WITH_TF) flush_tf(dtf_s, a.n_tf, pend_i, pend);
+      // near-opaque samples: correct the alpha adjoint by the true one
+      for (int k = 0; k < n_events; ++k) {
+        const OpaqueEvent& e = events[k];
+        const float4 R = suffix_composite(a, v, tf_s, ray, pixel, e);
+        const float gtrue = fmaf(g.w, R.w, -fmaf(g.x, R.x, fmaf(g.y, R.y, g.z * R.z)));
+        const float dd = e.oma * (gtrue - e.gA);  // change of dL/d(alpha of the sample)
+        if (dd == 0.f) continue;
+        const float xb = e.value * nf - 0.5f;
+        const float fl = floorf(xb);
+        const float wt = xb - fl;
+        const int i0 = (int)fl;
+        if (WITH_TF) {
+          if (i0 >= 0 && i0 < a.n_tf) atomicAdd(dtf_s + i0 * 4 + 3, (1.f - wt) * dd);
+          if (i0 + 1 >= 0 && i0 + 1 < a.n_tf) atomicAdd(dtf_s + (i0 + 1) * 4 + 3, wt * dd);
+        }
+        if (WITH_DENSITY) {
+          const int ic = min(max(i0, -2), a.n_tf);
+          const float dv = nf * dd * (tf_s[ic + 3].w - tf_s[ic + 2].w);
+          if (dv != 0.f) {
+            const DevBrick b = a.bricks[e.brick];
+            stencil_backward(b, a, e.brick, e.ux, e.uy, e.uz, dv, 0.f, 0.f, 0.f);
+          }
+        }
+      }
     }
   }
   count_samples(a.counter, nsamp);
