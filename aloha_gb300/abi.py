@@ -25,6 +25,7 @@ COMPOSITE_FP32, COMPOSITE_UBYTE = 0, 1
 ORDER_FACES, ORDER_REFERENCE_KD = 0, 1
 SPLIT_AUTO, SPLIT_PIXELS, SPLIT_RANKS = 0, 1, 2
 CHUNKS_AUTO, CHUNKS_RING, CHUNKS_PROBED = 0, 1, 2
+STAGING_NONE, STAGING_NEXT_SAMPLE = 0, 1
 
 # Every exported symbol of include/aloha.h (checked by the CPU test suite).
 EXPORTS = [
@@ -36,6 +37,7 @@ EXPORTS = [
     "aloha_batch_set_config", "aloha_batch_get_config", "aloha_batch_launch", "aloha_batch_launch_graph",
     "aloha_batch_autotune", "aloha_batch_destroy", "aloha_render_batch", "aloha_forward", "aloha_backward",
     "aloha_composite_over_noalloc", "aloha_set_render_tile", "aloha_set_render_split", "aloha_set_chunk_order",
+    "aloha_set_render_staging", "aloha_batch_set_staging", "aloha_batch_get_staging",
 ]
 
 
@@ -105,6 +107,9 @@ _SIGS = {
     "aloha_set_render_tile": ([P, I, I], I),
     "aloha_set_render_split": ([P, I], I),
     "aloha_set_chunk_order": ([P, I], I),
+    "aloha_set_render_staging": ([P, I], I),
+    "aloha_batch_set_staging": ([P, I], I),
+    "aloha_batch_get_staging": ([P, ctypes.POINTER(I)], I),
 }
 
 
@@ -258,6 +263,11 @@ class Context:
         first by a coarse probe); frames are bit-identical."""
         self._check(self._lib.aloha_set_chunk_order(self.h, int(mode)))
 
+    def set_render_staging(self, mode: int):
+        """STAGING_NONE or STAGING_NEXT_SAMPLE (the next sample's stencil rows
+        copied into shared memory with cp.async); frames are bit-identical."""
+        self._check(self._lib.aloha_set_render_staging(self.h, int(mode)))
+
     def set_render_split(self, mode: int):
         """SPLIT_AUTO, SPLIT_PIXELS (one thread per pixel over all ranks) or
         SPLIT_RANKS ((chunk, rank) work items); frames are bit-identical."""
@@ -327,6 +337,14 @@ class Batch:
         self.ctx._check(self.ctx._lib.aloha_batch_get_config(self.h, ctypes.byref(w), ctypes.byref(h),
                                                              ctypes.byref(c)))
         return w.value, h.value, c.value
+
+    def set_staging(self, stage: int):
+        self.ctx._check(self.ctx._lib.aloha_batch_set_staging(self.h, int(stage)))
+
+    def staging(self) -> int:
+        s = I()
+        self.ctx._check(self.ctx._lib.aloha_batch_get_staging(self.h, ctypes.byref(s)))
+        return s.value
 
     def launch(self, stream=None):
         self.ctx._check(self.ctx._lib.aloha_batch_launch(self.h, _stream(stream)))

@@ -1,9 +1,11 @@
-"""Ray-tile autotuner for the batched render with a JSON cache.
+"""Autotuner of the batched render with a JSON cache.
 
 The persistent batched kernel comes in four ray-tile shapes (8x4, 8x8, 16x8
-and 32x4 pixels per warp chunk); ``aloha_batch_autotune`` times each on the
-batch itself with CUDA events and keeps the fastest.  This module caches that choice per
-(GPU, batch configuration) in a JSON file so later processes skip the sweep.
+and 32x4 pixels per warp chunk), each with direct stencil loads or with the
+next sample's stencil rows staged in shared memory; ``aloha_batch_autotune``
+times all eight on the batch itself with CUDA events and keeps the fastest.
+This module caches that choice per (GPU, batch configuration) in a JSON file
+so later processes skip the sweep.
 """
 from __future__ import annotations
 
@@ -37,15 +39,16 @@ def _load(path: str) -> dict:
 
 
 def tune(batch, key: str, stream=None, reps: int = 2, path: str | None = None) -> dict:
-    """Apply the cached tile shape for `key`, or sweep, apply and cache it."""
+    """Apply the cached tile shape and staging for `key`, or sweep, apply and cache them."""
     path = path or cache_path()
     with _LOCK:
         entry = _load(path).get(key)
     if entry:
+        batch.set_staging(entry.get("staging", 0))
         batch.set_config(entry["tile_w"], entry["tile_h"], 0)
         return dict(entry, cached=True)
     w, h, ms = batch.autotune(stream, reps=reps)
-    entry = {"tile_w": w, "tile_h": h, "ms": ms}
+    entry = {"tile_w": w, "tile_h": h, "staging": batch.staging(), "ms": ms}
     with _LOCK:
         data = _load(path)
         data[key] = entry

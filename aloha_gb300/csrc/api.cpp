@@ -145,6 +145,8 @@ struct aloha_ctx {
   DeviceBuffer chunk_order;
   // rank-split render: mode, scratch rank images, per-chunk tickets, grid
   int split_mode = ALOHA_SPLIT_AUTO;
+  int staging = ALOHA_STAGING_NONE;  // stencil loads of the single-view render kernel
+  int grid_stage = -1;
   DeviceBuffer split_images, split_masks, split_items, split_done;
   int split_grid_n_tf = -1, split_grid_blocks = 0;
   int chunk_order_slots = -1;  // slot count of the chunk-order buffer's current layout
@@ -512,13 +514,14 @@ int launch_single(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
     cw = 8;
     ch = 4;
   }
-  if (c->grid_n_tf != c->n_tf || c->grid_cw != cw || c->grid_ch != ch) {
-    const int per_sm = render_blocks_per_sm(cw, ch, c->n_tf, false);
+  if (c->grid_n_tf != c->n_tf || c->grid_cw != cw || c->grid_ch != ch || c->grid_stage != c->staging) {
+    const int per_sm = render_blocks_per_sm(cw, ch, c->n_tf, false, c->staging);
     if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "render occupancy query failed");
     c->grid_blocks = per_sm * c->num_sms;
     c->grid_n_tf = c->n_tf;
     c->grid_cw = cw;
     c->grid_ch = ch;
+    c->grid_stage = c->staging;
   }
   BatchArgs b{};
   b.f = f;
@@ -539,7 +542,7 @@ int launch_single(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
   }
   const int warps_per_block = kRenderThreads / 32;
   const int grid = std::max(1, std::min(c->grid_blocks, (b.total_tiles + warps_per_block - 1) / warps_per_block));
-  CUDA_TRY(c, launch_render_warps(b, cw, ch, grid, false, s));
+  CUDA_TRY(c, launch_render_warps(b, cw, ch, grid, false, s, c->staging));
   return ALOHA_OK;
 }
 
@@ -984,6 +987,14 @@ int aloha_set_chunk_order(aloha_ctx* c, int mode) {
   if (mode != ALOHA_CHUNKS_AUTO && mode != ALOHA_CHUNKS_RING && mode != ALOHA_CHUNKS_PROBED)
     return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "chunk order %d not AUTO (0), RING (1) or PROBED (2)", mode);
   c->chunk_order_mode = mode;
+  return ALOHA_OK;
+}
+
+int aloha_set_render_staging(aloha_ctx* c, int mode) {
+  if (!c) return ALOHA_ERR_NULL_POINTER;
+  if (mode != ALOHA_STAGING_NONE && mode != ALOHA_STAGING_NEXT_SAMPLE)
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "staging %d not NONE (0) or NEXT_SAMPLE (1)", mode);
+  c->staging = mode;
   return ALOHA_OK;
 }
 

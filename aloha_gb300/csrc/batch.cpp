@@ -1,5 +1,5 @@
 // batch.cpp -- batched form: many views in one persistent launch, CUDA-graph
-// capture and the ray-tile autotuner.  No reference counterpart: the reference
+// capture and the autotuner over ray-tile shape and stencil staging.  No reference counterpart: the reference
 // renders one camera per owlLaunch2D (waikikiRenderer.cpp:1028).
 #include <cuda_runtime.h>
 
@@ -16,6 +16,7 @@ struct aloha_batch {
   std::vector<int> views;
   std::vector<uint32_t*> fbs;
   int tile_w = 16, tile_h = 8, ctas_per_sm = 0;
+  int stage = ALOHA_STAGING_NONE;
   int* d_view_ids = nullptr;
   uint32_t** d_fbs = nullptr;
   int* d_prefix = nullptr;
@@ -49,7 +50,7 @@ int configure(aloha_batch* b) {
   b->total_tiles = prefix.back();
   if (cudaMemcpy(b->d_prefix, prefix.data(), sizeof(int) * prefix.size(), cudaMemcpyHostToDevice) != cudaSuccess)
     return ctx_fail(c, ALOHA_ERR_CUDA, "batch: uploading tile prefix failed");
-  int per_sm = render_blocks_per_sm(b->tile_w, b->tile_h, ctx_n_tf(c), true);
+  int per_sm = render_blocks_per_sm(b->tile_w, b->tile_h, ctx_n_tf(c), true, b->stage);
   if (per_sm <= 0) return ctx_fail(c, ALOHA_ERR_CUDA, "batch: occupancy query failed");
   if (b->ctas_per_sm > 0 && b->ctas_per_sm < per_sm) per_sm = b->ctas_per_sm;
   b->grid = ctx_num_sms(c) * per_sm;
@@ -70,7 +71,7 @@ int enqueue(aloha_batch* b, cudaStream_t s) {
   if (cudaMemsetAsync(b->d_work, 0, sizeof(unsigned int), s) != cudaSuccess ||
       cudaMemsetAsync(a.f.counter, 0, sizeof(unsigned long long), s) != cudaSuccess)
     return ctx_fail(c, ALOHA_ERR_CUDA, "batch: memset failed");
-  cudaError_t e = launch_render_warps(a, b->tile_w, b->tile_h, b->grid, true, s);
+  cudaError_t e = launch_render_warps(a, b->tile_w, b->tile_h, b->grid, true, s, b->stage);
   if (e != cudaSuccess) return ctx_fail(c, ALOHA_ERR_CUDA, "batch launch: %s", cudaGetErrorString(e));
   ctx_mark_samples(c);
   return ALOHA_OK;
@@ -138,6 +139,20 @@ int aloha_batch_set_config(aloha_batch* b, int tile_w, int tile_h, int ctas_per_
   return configure(b);
 }
 
+int aloha_batch_set_staging(aloha_batch* b, int stage) {
+  if (!b) return ALOHA_ERR_NULL_POINTER;
+  if (stage != ALOHA_STAGING_NONE && stage != ALOHA_STAGING_NEXT_SAMPLE)
+    return ctx_fail(b->ctx, ALOHA_ERR_INVALID_ARGUMENT, "staging %d not NONE (0) or NEXT_SAMPLE (1)", stage);
+  b->stage = stage;
+  return configure(b);
+}
+
+int aloha_batch_get_staging(const aloha_batch* b, int* stage) {
+  if (!b || !stage) return ALOHA_ERR_NULL_POINTER;
+  *stage = b->stage;
+  return ALOHA_OK;
+}
+
 int aloha_batch_get_config(const aloha_batch* b, int* tile_w, int* tile_h, int* ctas_per_sm) {
   if (!b || !tile_w || !tile_h || !ctas_per_sm) return ALOHA_ERR_NULL_POINTER;
   *tile_w = b->tile_w;
@@ -196,9 +211,12 @@ int aloha_batch_autotune(aloha_batch* b, void* stream, int reps, int* tile_w, in
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     return ctx_fail(b->ctx, ALOHA_ERR_CUDA, "cudaEventCreate failed");
   float best = -1.f;
-  int bw = b->tile_w, bh = b->tile_h;
+  int bw = b->tile_w, bh = b->tile_h, bs = b->stage;
   int rc = ALOHA_OK;
-  for (auto& sh : shapes) {
+  for (int k = 0; k < 8 && !rc; ++k) {
+    const int* sh = shapes[k % 4];
+    const int stage = k / 4;  // ALOHA_STAGING_NONE, then ALOHA_STAGING_NEXT_SAMPLE
+    b->stage = stage;
     rc = aloha_batch_set_config(b, sh[0], sh[1], 0);
     if (rc) break;
     rc = aloha_batch_launch(b, stream);  // warm-up
@@ -218,11 +236,13 @@ int aloha_batch_autotune(aloha_batch* b, void* stream, int reps, int* tile_w, in
       best = t;
       bw = sh[0];
       bh = sh[1];
+      bs = stage;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc) return rc;
+  b->stage = bs;
   rc = aloha_batch_set_config(b, bw, bh, 0);
   if (rc) return rc;
   *tile_w = bw;

@@ -154,7 +154,9 @@ cudaError_t launch_pad_brick(const float* src, int nx, int ny, int nz, float4* d
                              int* nonfinite_flag, cudaStream_t s);
 // Persistent render launch; `batch` selects the instance tuned for batches.
 constexpr int kSingleRenderBlocks = 5, kBatchRenderBlocks = 7;  // CTAs per SM
-cudaError_t launch_render_warps(const BatchArgs& a, int chunk_w, int chunk_h, int grid, bool batch, cudaStream_t s);
+// `stage`: ALOHA_STAGING_NONE or _NEXT_SAMPLE (the stencil loads).
+cudaError_t launch_render_warps(const BatchArgs& a, int chunk_w, int chunk_h, int grid, bool batch, cudaStream_t s,
+                                int stage = ALOHA_STAGING_NONE);
 cudaError_t launch_macrocell_range(const DevBrick& b, float2* out, cudaStream_t s);
 cudaError_t launch_macrocell_empty(const float2* ranges, int count, const int* prefix, int n, uint8_t* empty,
                                    cudaStream_t s);
@@ -163,7 +165,7 @@ inline int macrocells(const DevBrick& b) {
          ((b.n[2] + kMacro - 1) >> kMacroShift);
 }
 // CTAs of the render kernel that fit on one SM for a chunk shape (0 if the shape is unknown).
-int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf, bool batch);
+int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf, bool batch, int stage = ALOHA_STAGING_NONE);
 // `many_ranks` selects the instance tuned for many short (chunk, rank) items.
 constexpr int kManyRankSplitBlocks = 7;  // CTAs per SM
 cudaError_t launch_render_split(const SplitArgs& a, int grid, bool many_ranks, cudaStream_t s);

@@ -89,41 +89,18 @@ struct StencilOut {
   float value, gx, gy, gz;
 };
 
-__device__ __forceinline__ StencilOut stencil(const float4* __restrict__ base, int sy, int sz, int nx, int ny,
-                                              int nz, float ux, float uy, float uz) {
-  const float mx = ux - 0.5f, my = uy - 0.5f, mz = uz - 0.5f;
-  const float fmx = floorf(mx), fmy = floorf(my), fmz = floorf(mz);
-  const float fcx = floorf(ux), fcy = floorf(uy), fcz = floorf(uz);
-  const float fx = mx - fmx, fy = my - fmy, fz = mz - fmz;  // weights of the displaced taps
-  const float gx = ux - fcx, gy = uy - fcy, gz = uz - fcz;  // weights of the centre
-  const bool hx = fcx != fmx, hy = fcy != fmy, hz = fcz != fmz;  // floor(u) == floor(u - 1/2) + 1
-  // Indices, clamped into the apron.  Every index the oracle clamps to the
-  // edge maps to an apron voxel holding that edge value, so these clamps only
-  // keep pathological coordinates in bounds and never change a value.
-  const int ix = min(max((int)fmx, -kApron), nx - 1);
-  const int iy = min(max((int)fmy, -kApron), ny - 1);
-  const int iz = min(max((int)fmz, -kApron), nz - 1);
-  const int cx = min(max((int)fcx, -kApron), nx);
-  const int cy = min(max((int)fcy, -kApron), ny);
-  const int cz = min(max((int)fcz, -kApron), nz);
-
-  // X region: x in {ix, ix+1, ix+2}, y in {cy, cy+1}, z in {cz, cz+1}: one
-  // quad per (y, z) row.
-  const float4* p0 = base + (cz * sz + cy * sy + ix);
-  const float4 r00 = __ldg(p0), r10 = __ldg(p0 + sy), r01 = __ldg(p0 + sz), r11 = __ldg(p0 + sz + sy);
+// The stencil's arithmetic from its eight loaded rows (shared by the direct
+// loads of stencil() and the staged loads of StagedLoads, so both give the
+// same bits).
+__device__ __forceinline__ StencilOut stencil_rows(const float4 r00, const float4 r10, const float4 r01,
+                                                   const float4 r11, const float2 e0, const float2 e1,
+                                                   const float2 f0, const float2 f1, float fx, float fy, float fz,
+                                                   float gx, float gy, float gz, bool hx, bool hy, bool hz) {
   const float a000 = r00.x, a100 = r00.y, a200 = r00.z;
   const float a010 = r10.x, a110 = r10.y, a210 = r10.z;
   const float a001 = r01.x, a101 = r01.y, a201 = r01.z;
   const float a011 = r11.x, a111 = r11.y, a211 = r11.z;
-  // Extra y row (iy or iy+2) and extra z slice (iz or iz+2) at x in {cx, cx+1}:
-  // the first half of a quad.
-  const int ye = hy ? iy : iy + 2;
-  const int ze = hz ? iz : iz + 2;
-  const float4* p1 = base + (cz * sz + ye * sy + cx);
-  const float2 e0 = __ldg(reinterpret_cast<const float2*>(p1)), e1 = __ldg(reinterpret_cast<const float2*>(p1 + sz));
   const float b00 = e0.x, b10 = e0.y, b01 = e1.x, b11 = e1.y;
-  const float4* p2 = base + (ze * sz + cy * sy + cx);
-  const float2 f0 = __ldg(reinterpret_cast<const float2*>(p2)), f1 = __ldg(reinterpret_cast<const float2*>(p2 + sy));
   const float c00 = f0.x, c10 = f0.y, c01 = f1.x, c11 = f1.y;
 
   // x taps: columns X_k = bilinear (y by gy, then z by gz) at x = ix + k.
@@ -160,6 +137,160 @@ __device__ __forceinline__ StencilOut stencil(const float4* __restrict__ base, i
   s.gz = lerpf(Z1, Z2, fz) - lerpf(Z0, Z1, fz);
   return s;
 }
+
+__device__ __forceinline__ StencilOut stencil(const float4* __restrict__ base, int sy, int sz, int nx, int ny,
+                                              int nz, float ux, float uy, float uz) {
+  const float mx = ux - 0.5f, my = uy - 0.5f, mz = uz - 0.5f;
+  const float fmx = floorf(mx), fmy = floorf(my), fmz = floorf(mz);
+  const float fcx = floorf(ux), fcy = floorf(uy), fcz = floorf(uz);
+  const float fx = mx - fmx, fy = my - fmy, fz = mz - fmz;  // weights of the displaced taps
+  const float gx = ux - fcx, gy = uy - fcy, gz = uz - fcz;  // weights of the centre
+  const bool hx = fcx != fmx, hy = fcy != fmy, hz = fcz != fmz;  // floor(u) == floor(u - 1/2) + 1
+  // Indices, clamped into the apron.  Every index the oracle clamps to the
+  // edge maps to an apron voxel holding that edge value, so these clamps only
+  // keep pathological coordinates in bounds and never change a value.
+  const int ix = min(max((int)fmx, -kApron), nx - 1);
+  const int iy = min(max((int)fmy, -kApron), ny - 1);
+  const int iz = min(max((int)fmz, -kApron), nz - 1);
+  const int cx = min(max((int)fcx, -kApron), nx);
+  const int cy = min(max((int)fcy, -kApron), ny);
+  const int cz = min(max((int)fcz, -kApron), nz);
+
+  // X region: x in {ix, ix+1, ix+2}, y in {cy, cy+1}, z in {cz, cz+1}: one
+  // quad per (y, z) row.
+  const float4* p0 = base + (cz * sz + cy * sy + ix);
+  const float4 r00 = __ldg(p0), r10 = __ldg(p0 + sy), r01 = __ldg(p0 + sz), r11 = __ldg(p0 + sz + sy);
+  // Extra y row (iy or iy+2) and extra z slice (iz or iz+2) at x in {cx, cx+1}:
+  // the first half of a quad.
+  const int ye = hy ? iy : iy + 2;
+  const int ze = hz ? iz : iz + 2;
+  const float4* p1 = base + (cz * sz + ye * sy + cx);
+  const float2 e0 = __ldg(reinterpret_cast<const float2*>(p1)), e1 = __ldg(reinterpret_cast<const float2*>(p1 + sz));
+  const float4* p2 = base + (ze * sz + cy * sy + cx);
+  const float2 f0 = __ldg(reinterpret_cast<const float2*>(p2)), f1 = __ldg(reinterpret_cast<const float2*>(p2 + sy));
+  return stencil_rows(r00, r10, r01, r11, e0, e1, f0, f1, fx, fy, fz, gx, gy, gz, hx, hy, hz);
+}
+
+// ---- Where the stencil's rows come from -----------------------------------
+// DirectLoads: read-only loads from the brick when the sample is evaluated.
+// StagedLoads: the rows of the next sample along the ray are copied into this
+// thread's own shared-memory slots with cp.async while the current sample is
+// evaluated (double buffering), so the gather's latency overlaps the
+// arithmetic without holding registers.  Each thread stages only for itself,
+// so no warp or CTA synchronisation is involved; a staged sample is used only
+// when the march reaches exactly its t within the same brick march (t is
+// strictly increasing there), else it is dropped.  The values are the same
+// as the direct loads', so frames are bit-identical.
+struct DirectLoads {
+  static constexpr bool kStaged = false;
+  __device__ __forceinline__ void begin_brick() {}
+  __device__ __forceinline__ void finish() {}
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Shared memory of the staged loads: [2 slots][6 rows][kRenderThreads] float4
+// (each thread's rows strided by the CTA size, so a warp's row reads are
+// contiguous); rows 0-3 are the x-region quads, row 4 the extra y row's two
+// halves, row 5 the extra z slice's.
+constexpr int kStageRows = 6;
+constexpr size_t kStageBytes = (size_t)2 * kStageRows * kRenderThreads * sizeof(float4);
+
+struct StagedLoads {
+  static constexpr bool kStaged = true;
+  float4* col;     // this thread's column: row e of slot k at col[(k * kStageRows + e) * kRenderThreads]
+  float t_staged;  // t of the sample in slot `cur` (NaN: none)
+  int cur;
+  bool inflight;   // copies may be outstanding
+  __device__ __forceinline__ void init(float4* stage_smem) {
+    col = stage_smem + threadIdx.x;
+    t_staged = __int_as_float(0x7fffffff);
+    cur = 0;
+    inflight = false;
+  }
+  __device__ __forceinline__ void begin_brick() { t_staged = __int_as_float(0x7fffffff); }
+  // Outstanding copies must land before the CTA's shared memory is released.
+  __device__ __forceinline__ void finish() {
+    if (inflight) cp_async_wait_all();
+    inflight = false;
+  }
+  __device__ __forceinline__ float4* row(int slot, int e) const { return col + (slot * kStageRows + e) * kRenderThreads; }
+
+  // Starts the copies of the stencil rows at (ux, uy, uz) into `slot`: the
+  // addresses of stencil(), clamped into the apron.
+  __device__ __forceinline__ void issue(int slot, const float4* __restrict__ base, int sy, int sz, int nx, int ny,
+                                        int nz, float ux, float uy, float uz) const {
+    const float fmx = floorf(ux - 0.5f), fmy = floorf(uy - 0.5f), fmz = floorf(uz - 0.5f);
+    const float fcx = floorf(ux), fcy = floorf(uy), fcz = floorf(uz);
+    const int ix = min(max((int)fmx, -kApron), nx - 1);
+    const int iy = min(max((int)fmy, -kApron), ny - 1);
+    const int iz = min(max((int)fmz, -kApron), nz - 1);
+    const int cx = min(max((int)fcx, -kApron), nx);
+    const int cy = min(max((int)fcy, -kApron), ny);
+    const int cz = min(max((int)fcz, -kApron), nz);
+    const int ye = fcy != fmy ? iy : iy + 2;
+    const int ze = fcz != fmz ? iz : iz + 2;
+    const float4* p0 = base + (cz * sz + cy * sy + ix);
+    const float4* p1 = base + (cz * sz + ye * sy + cx);
+    const float4* p2 = base + (ze * sz + cy * sy + cx);
+    cp_async16(row(slot, 0), p0);
+    cp_async16(row(slot, 1), p0 + sy);
+    cp_async16(row(slot, 2), p0 + sz);
+    cp_async16(row(slot, 3), p0 + sz + sy);
+    float2* e = reinterpret_cast<float2*>(row(slot, 4));
+    float2* f = reinterpret_cast<float2*>(row(slot, 5));
+    cp_async8(e, p1);
+    cp_async8(e + 1, p1 + sz);
+    cp_async8(f, p2);
+    cp_async8(f + 1, p2 + sy);
+    cp_async_commit();
+  }
+
+  // The sample at t (voxel coordinate u): its rows from the slot it was
+  // staged in (or loaded now), after starting the copies of the next sample
+  // t + dt when that one lies before t1.
+  __device__ __forceinline__ StencilOut sample(const float4* __restrict__ base, int sy, int sz, int nx, int ny, int nz,
+                                               float ux, float uy, float uz, float t, float t1, float dt,
+                                               const float o[3], const float d[3], float lox, float loy, float loz) {
+    if (!(t_staged == t)) {
+      if (inflight) cp_async_wait_all();  // a dropped copy may still be landing in `cur`
+      issue(cur, base, sy, sz, nx, ny, nz, ux, uy, uz);
+    }
+    const float tn = t + dt;  // the march's next t, by the same addition
+    const bool next = tn < t1;
+    if (next) {
+      issue(cur ^ 1, base, sy, sz, nx, ny, nz, fmaf(tn, d[0], o[0]) - lox, fmaf(tn, d[1], o[1]) - loy,
+            fmaf(tn, d[2], o[2]) - loz);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    const float4 r00 = *row(cur, 0), r10 = *row(cur, 1), r01 = *row(cur, 2), r11 = *row(cur, 3);
+    const float4 ef = *row(cur, 4), ff = *row(cur, 5);
+    const float mx = ux - 0.5f, my = uy - 0.5f, mz = uz - 0.5f;
+    const float fmx = floorf(mx), fmy = floorf(my), fmz = floorf(mz);
+    const float fcx = floorf(ux), fcy = floorf(uy), fcz = floorf(uz);
+    const StencilOut s = stencil_rows(r00, r10, r01, r11, make_float2(ef.x, ef.y), make_float2(ef.z, ef.w),
+                                      make_float2(ff.x, ff.y), make_float2(ff.z, ff.w), mx - fmx, my - fmy, mz - fmz,
+                                      ux - fcx, uy - fcy, uz - fcz, fcx != fmx, fcy != fmy, fcz != fmz);
+    t_staged = next ? tn : __int_as_float(0x7fffffff);
+    inflight = next;
+    cur ^= 1;
+    return s;
+  }
+};
 
 // tex1D on the transfer function (linear, normalized coords, border 0;
 // waikikiRenderer.cpp:990-1008).  tf_s holds the n entries at [2, n+2) with
@@ -205,10 +336,10 @@ struct NoHook {
 
 // integrateBrick (deviceCode.cpp:256-298) over [t0, t1); returns the number
 // of samples taken.
-template <class Hook>
+template <class Hook, class Loads = DirectLoads>
 __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
                                                 const Ray& r, float t0, float t1, float ils, float dt, float et,
-                                                float4& color, Hook& hook) {
+                                                float4& color, Hook& hook, Loads& loads) {
   const float4* __restrict__ base = b.base;
   const int sy = b.sy, sz = b.sz, nx = b.n[0], ny = b.n[1], nz = b.n[2];
   const float lox = b.lo[0], loy = b.lo[1], loz = b.lo[2];
@@ -233,6 +364,7 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
   // in an empty macrocell leaves the colour unchanged as well), so the bound
   // only has to be right for speed.
   float t_cell = t0;
+  loads.begin_brick();
   while (t < t1 && color.w < et && n < cap) {
     const float ux = fmaf(t, r.d[0], r.o[0]) - lox;
     const float uy = fmaf(t, r.d[1], r.o[1]) - loy;
@@ -302,13 +434,25 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
     }
     hook(t, n, color);
     ++n;
-    const StencilOut s = stencil(base, sy, sz, nx, ny, nz, ux, uy, uz);
+    StencilOut s;
+    if constexpr (Loads::kStaged)
+      s = loads.sample(base, sy, sz, nx, ny, nz, ux, uy, uz, t, t1, dt, r.o, r.d, lox, loy, loz);
+    else
+      s = stencil(base, sy, sz, nx, ny, nz, ux, uy, uz);
     const float shade = shade_factor(s, r);
     const float4 c = tf_lookup(tf_s, n_tf, nf, s.value);
     composite_step(color, c, shade);
     t = t + dt;
   }
   return n;
+}
+
+template <class Hook>
+__device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
+                                                const Ray& r, float t0, float t1, float ils, float dt, float et,
+                                                float4& color, Hook& hook) {
+  DirectLoads direct;
+  return march_brick(b, tf_s, n_tf, r, t0, t1, ils, dt, et, color, hook, direct);
 }
 
 __device__ __forceinline__ float saturatef_(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
@@ -346,9 +490,10 @@ __device__ __forceinline__ void load_tf(float4* tf_s, const float4* __restrict__
 // rank's bricks [j0, j1) of the view schedule front to back, spp draws, early
 // termination on the rank's own alpha.  Returns the spp sum of the colours;
 // z = nearest brick entry / max depth, ns = samples taken.
+template <class Loads = DirectLoads>
 __device__ __forceinline__ float4 march_rank(const FrameArgs& a, const DevView& v, const float4* tf_s, const Ray& ray,
                                              const int* __restrict__ rbricks, int j0, int j1, int pixel, float& z,
-                                             uint32_t& ns) {
+                                             uint32_t& ns, Loads& loads) {
   float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
   uint32_t draw = 0;
   for (int s = 0; s < a.spp; ++s) {
@@ -362,7 +507,7 @@ __device__ __forceinline__ float4 march_rank(const FrameArgs& a, const DevView& 
       const float tnear = (t0 > tmin ? t0 : 0.0f) + tmin;
       z = fminf(z, tnear / v.max_depth);
       NoHook none;
-      ns += march_brick(b, tf_s, a.n_tf, ray, t0, t1, ils, a.dt, a.et_alpha, color, none);
+      ns += march_brick(b, tf_s, a.n_tf, ray, t0, t1, ils, a.dt, a.et_alpha, color, none, loads);
       tmin = t1 + 1e-20f;
       if (!(color.w < a.et_alpha)) break;
     }
@@ -455,8 +600,9 @@ __device__ __forceinline__ bool pixel_in_island(const FrameArgs& a, int W, int x
 // One pixel of one view: every virtual rank marches its bricks and runs
 // renderFrame's output stage; the rank images are blended front to back.
 // Returns the number of samples.
+template <class Loads = DirectLoads>
 __device__ __forceinline__ uint32_t render_pixel(const FrameArgs& a, const DevView& v, const float4* tf_s, int x,
-                                                 int y, uint32_t* fb_out, size_t fb_index) {
+                                                 int y, uint32_t* fb_out, size_t fb_index, Loads& loads) {
   const int W = v.width, H = v.height;
   const int pixel = x + W * y;
   const size_t npx = (size_t)W * H;
@@ -473,7 +619,8 @@ __device__ __forceinline__ uint32_t render_pixel(const FrameArgs& a, const DevVi
     float z = 1.0f;
     uint32_t ns = 0;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (in_island) acc = march_rank(a, v, tf_s, ray, rbricks, __ldg(rstart + r), __ldg(rstart + r + 1), pixel, z, ns);
+    if (in_island)
+      acc = march_rank(a, v, tf_s, ray, rbricks, __ldg(rstart + r), __ldg(rstart + r + 1), pixel, z, ns, loads);
     blend.add(a.composite_mode, rank_output(a, W, H, r, x, y, pixel, npx, acc, ns, z, a.rank_images, a.rank_depth));
     total += ns;
   }

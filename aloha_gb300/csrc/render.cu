@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "internal.h"
 #include "march.cuh"
 
@@ -20,11 +22,17 @@ namespace aloha {
 // chunks, which run faster with more registers per thread (5 CTAs, 96
 // registers); a batch of views is throughput-bound and runs faster with more
 // resident warps (7 CTAs, 72 registers).
-template <int CW, int CH, int MINB>
+// STAGE selects the stencil loads: 0 direct, 1 the next sample's rows staged
+// in shared memory with cp.async (StagedLoads; shared memory after the
+// transfer function).
+template <int CW, int CH, int MINB, int STAGE>
 __global__ void __launch_bounds__(kRenderThreads, MINB) render_warps_kernel(BatchArgs b) {
   extern __shared__ float4 tf_s[];
   load_tf(tf_s, b.f.tf, b.f.n_tf);
   __syncthreads();
+  using Loads = typename std::conditional<STAGE == 1, StagedLoads, DirectLoads>::type;
+  Loads loads;
+  if constexpr (STAGE == 1) loads.init(tf_s + (b.f.n_tf + 4));
   const int lane = threadIdx.x & 31;
   uint32_t n = 0;
   for (;;) {
@@ -62,9 +70,11 @@ __global__ void __launch_bounds__(kRenderThreads, MINB) render_warps_kernel(Batc
     for (int sub = 0; sub < (CW / 8) * (CH / 4); ++sub) {
       const int x = x0 + (sub % (CW / 8)) * 8 + (lane & 7);
       const int y = y0 + (sub / (CW / 8)) * 4 + (lane >> 3);
-      if (x < v.width && y < v.height) n += render_pixel(b.f, v, tf_s, x, y, fb, (size_t)x + (size_t)v.width * y);
+      if (x < v.width && y < v.height)
+        n += render_pixel(b.f, v, tf_s, x, y, fb, (size_t)x + (size_t)v.width * y, loads);
     }
   }
+  loads.finish();
   count_samples(b.f.counter, n);
 }
 
@@ -260,9 +270,10 @@ __global__ void __launch_bounds__(kRenderThreads, MINB) render_split_kernel(Spli
         float z = 1.0f;
         uint32_t ns = 0;
         float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        DirectLoads direct;
         if (pixel_in_island(s.f, W, x, y))
           acc = march_rank(s.f, v, tf_s, generate_ray(v, x, y), rbricks, __ldg(rstart + r), __ldg(rstart + r + 1),
-                           pixel, z, ns);
+                           pixel, z, ns, direct);
         rank_output(s.f, W, H, r, x, y, pixel, npx, acc, ns, z, planes, nullptr);
         n += ns;
       }
@@ -381,6 +392,7 @@ __global__ void macrocell_empty_kernel(const float2* __restrict__ ranges, int co
 }
 
 static size_t tf_smem(int n_tf) { return (size_t)(n_tf + 4) * sizeof(float4); }
+static size_t render_smem(int n_tf, int stage) { return tf_smem(n_tf) + (stage ? kStageBytes : 0); }
 
 cudaError_t launch_macrocell_range(const DevBrick& b, float2* out, cudaStream_t s) {
   const int mnx = (b.n[0] + kMacro - 1) >> kMacroShift, mny = (b.n[1] + kMacro - 1) >> kMacroShift,
@@ -401,35 +413,41 @@ cudaError_t launch_macrocell_empty(const float2* ranges, int count, const int* p
 
 namespace {
 
-// The kernel instance for a chunk shape and launch mode, or null.
+// The kernel instance for a chunk shape, launch mode and staging, or null.
 using RenderKernel = void (*)(BatchArgs);
-template <int MINB>
+template <int MINB, int STAGE>
 RenderKernel render_kernel_for(int chunk_w, int chunk_h) {
-  if (chunk_w == 8 && chunk_h == 4) return render_warps_kernel<8, 4, MINB>;
-  if (chunk_w == 8 && chunk_h == 8) return render_warps_kernel<8, 8, MINB>;
-  if (chunk_w == 16 && chunk_h == 8) return render_warps_kernel<16, 8, MINB>;
-  if (chunk_w == 32 && chunk_h == 4) return render_warps_kernel<32, 4, MINB>;
+  if (chunk_w == 8 && chunk_h == 4) return render_warps_kernel<8, 4, MINB, STAGE>;
+  if (chunk_w == 8 && chunk_h == 8) return render_warps_kernel<8, 8, MINB, STAGE>;
+  if (chunk_w == 16 && chunk_h == 8) return render_warps_kernel<16, 8, MINB, STAGE>;
+  if (chunk_w == 32 && chunk_h == 4) return render_warps_kernel<32, 4, MINB, STAGE>;
   return nullptr;
 }
 
-RenderKernel render_kernel(int chunk_w, int chunk_h, bool batch) {
-  return batch ? render_kernel_for<kBatchRenderBlocks>(chunk_w, chunk_h)
-               : render_kernel_for<kSingleRenderBlocks>(chunk_w, chunk_h);
+RenderKernel render_kernel(int chunk_w, int chunk_h, bool batch, int stage) {
+  if (stage == ALOHA_STAGING_NEXT_SAMPLE)
+    return batch ? render_kernel_for<kBatchRenderBlocks, 1>(chunk_w, chunk_h)
+                 : render_kernel_for<kSingleRenderBlocks, 1>(chunk_w, chunk_h);
+  if (stage != ALOHA_STAGING_NONE) return nullptr;
+  return batch ? render_kernel_for<kBatchRenderBlocks, 0>(chunk_w, chunk_h)
+               : render_kernel_for<kSingleRenderBlocks, 0>(chunk_w, chunk_h);
 }
 
 }  // namespace
 
-cudaError_t launch_render_warps(const BatchArgs& b, int chunk_w, int chunk_h, int grid, bool batch, cudaStream_t s) {
-  const RenderKernel k = render_kernel(chunk_w, chunk_h, batch);
+cudaError_t launch_render_warps(const BatchArgs& b, int chunk_w, int chunk_h, int grid, bool batch, cudaStream_t s,
+                                int stage) {
+  const RenderKernel k = render_kernel(chunk_w, chunk_h, batch, stage);
   if (!k) return cudaErrorInvalidValue;
-  k<<<grid, kRenderThreads, tf_smem(b.f.n_tf), s>>>(b);
+  k<<<grid, kRenderThreads, render_smem(b.f.n_tf, stage), s>>>(b);
   return cudaGetLastError();
 }
 
-int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf, bool batch) {
-  const RenderKernel k = render_kernel(chunk_w, chunk_h, batch);
+int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf, bool batch, int stage) {
+  const RenderKernel k = render_kernel(chunk_w, chunk_h, batch, stage);
   int n = 0;
-  if (!k || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kRenderThreads, tf_smem(n_tf)) != cudaSuccess) {
+  if (!k || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kRenderThreads, render_smem(n_tf, stage)) !=
+                cudaSuccess) {
     cudaGetLastError();
     return 0;
   }

@@ -329,16 +329,19 @@ def main():
 
     # work-division sweep of the single-view render (untimed): the pixel split
     # at three chunk shapes, and the (chunk, rank) split
-    schedules = {"pixels 8x4": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_PROBED),
-                 "pixels 8x4 ring order": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_RING),
-                 "pixels 8x8": (abi.SPLIT_PIXELS, 8, 8, abi.CHUNKS_PROBED),
-                 "pixels 16x8": (abi.SPLIT_PIXELS, 16, 8, abi.CHUNKS_PROBED),
-                 "ranks": (abi.SPLIT_RANKS, 0, 0, abi.CHUNKS_AUTO)}
+    none, staged = abi.STAGING_NONE, abi.STAGING_NEXT_SAMPLE
+    schedules = {"pixels 8x4": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_PROBED, none),
+                 "pixels 8x4 staged": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_PROBED, staged),
+                 "pixels 8x4 ring order": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_RING, none),
+                 "pixels 8x8": (abi.SPLIT_PIXELS, 8, 8, abi.CHUNKS_PROBED, none),
+                 "pixels 16x8": (abi.SPLIT_PIXELS, 16, 8, abi.CHUNKS_PROBED, none),
+                 "ranks": (abi.SPLIT_RANKS, 0, 0, abi.CHUNKS_AUTO, none)}
     sched_ms = {}
-    for name, (split, tw, th, chunks) in schedules.items():
+    for name, (split, tw, th, chunks, stage) in schedules.items():
         ctx.set_render_split(split)
         ctx.set_render_tile(tw, th)
         ctx.set_chunk_order(chunks)
+        ctx.set_render_staging(stage)
         probe = mine[:8]
         for ci in probe[:2]:
             ctx.set_camera(0, *cams[ci])
@@ -354,11 +357,12 @@ def main():
             ms += e0.elapsed_time(e1)
         sched_ms[name] = ms / len(probe)
     best = min(sched_ms, key=sched_ms.get)
-    split, tw, th, chunks = schedules[best]
+    split, tw, th, chunks, stage = schedules[best]
     ctx.set_render_split(split)
     ctx.set_render_tile(tw, th)
     ctx.set_chunk_order(chunks)
-    kernel = "render_split_kernel" if split == abi.SPLIT_RANKS else f"render_warps_kernel<{tw},{th}>"
+    ctx.set_render_staging(stage)
+    kernel = "render_split_kernel" if split == abi.SPLIT_RANKS else f"render_warps_kernel<{tw},{th},5,{stage}>"
     # our kernels per frame: the render, plus the chunk probe (which also
     # counts the classes), scan and scatter of the cost order, and for the
     # rank split its mask, three scan kernels and emit
@@ -569,6 +573,8 @@ def batched_section(ctx, cams, mine, W, H, args, stream, dev, samples_of):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
+    stage = b.staging()
+    by_stage = staging_sweep(b, stream, timed)
     ms_graph = timed(lambda: b.launch_graph(stream))
 
     def plain():
@@ -578,8 +584,24 @@ def batched_section(ctx, cams, mine, W, H, args, stream, dev, samples_of):
     ms_plain = timed(plain)
     samples = sum(samples_of[ci] for ci in mine[:nv])
     b.close()
-    return {"views": nv, "tile": [tw, th], "ms_batch": ms_graph, "ms_plain_launches": ms_plain,
+    return {"views": nv, "tile": [tw, th], "staging": STAGING_NAMES[stage], "ms_batch_by_staging": by_stage,
+            "ms_batch": ms_graph, "ms_plain_launches": ms_plain,
             "speedup_vs_plain": ms_plain / ms_graph, "gsamples_per_s": samples / (ms_graph * 1e-3) / 1e9}
+
+
+STAGING_NAMES = {0: "none", 1: "next sample (cp.async, shared memory)"}
+
+
+def staging_sweep(b, stream, timed):
+    """Graph-launch time of the batch at its tuned tile with each staging
+    (untimed for the headline); leaves the tuned staging set."""
+    chosen = b.staging()
+    out = {}
+    for stage, name in STAGING_NAMES.items():
+        b.set_staging(stage)
+        out[name] = timed(lambda: b.launch_graph(stream))
+    b.set_staging(chosen)
+    return out
 
 
 def uneven_batched_section(vol, dev, big=64, small=32):
@@ -625,13 +647,16 @@ def uneven_batched_section(vol, dev, big=64, small=32):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
+    stage = b.staging()
+    by_stage = staging_sweep(b, stream, timed)
     ms_batch = timed(lambda: b.launch_graph(stream))
     ms_plain = timed(lambda: [ctx.render(v, f, stream) for v, f in enumerate(fbs)])
     b.close()
     ctx.close()
     px = sum(w * w for w in sizes)
     return {"config": f"{n}^3 in {len(descs)} uneven bricks, {big} views at 1024^2 + {small} at 512^2",
-            "tile": [tw, th], "ms_batch": ms_batch, "ms_plain_launches": ms_plain,
+            "tile": [tw, th], "staging": STAGING_NAMES[stage], "ms_batch_by_staging": by_stage,
+            "ms_batch": ms_batch, "ms_plain_launches": ms_plain,
             "speedup_vs_plain": ms_plain / ms_batch, "gsamples_per_s": samples / (ms_batch * 1e-3) / 1e9,
             "ms_per_megapixel": ms_batch / (px / 2**20)}
 

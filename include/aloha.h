@@ -48,6 +48,7 @@ enum { ALOHA_COMPOSITE_FP32 = 0, ALOHA_COMPOSITE_UBYTE = 1 };
 enum { ALOHA_ORDER_FACES = 0, ALOHA_ORDER_REFERENCE_KD = 1 };
 enum { ALOHA_SPLIT_AUTO = 0, ALOHA_SPLIT_PIXELS = 1, ALOHA_SPLIT_RANKS = 2 };
 enum { ALOHA_CHUNKS_AUTO = 0, ALOHA_CHUNKS_RING = 1, ALOHA_CHUNKS_PROBED = 2 };
+enum { ALOHA_STAGING_NONE = 0, ALOHA_STAGING_NEXT_SAMPLE = 1 };
 
 typedef struct aloha_ctx aloha_ctx;
 
@@ -167,6 +168,15 @@ int aloha_set_render_split(aloha_ctx* ctx, int mode);
  * short already).  No reference counterpart. */
 int aloha_set_chunk_order(aloha_ctx* ctx, int mode);
 
+/* Where the single-view render kernel takes each sample's stencil rows from:
+ * ALOHA_STAGING_NONE (the default) loads them from the brick when the sample
+ * is evaluated; ALOHA_STAGING_NEXT_SAMPLE copies the next sample's rows into
+ * the thread's own shared-memory slots with cp.async while the current
+ * sample is evaluated (double buffering, 24 KB of shared memory per CTA).
+ * Frames are bit-identical either way.  No reference counterpart (the
+ * reference samples 3D textures, deviceCode.cpp:279-289). */
+int aloha_set_render_staging(aloha_ctx* ctx, int mode);
+
 /* Render one view into an RGBA8 frame buffer of width*height uint32
  * (Renderer::render, waikikiRenderer.cpp:1015-1080): all virtual ranks march
  * their bricks and their images are composited in one fused kernel.  fb may
@@ -228,10 +238,15 @@ int aloha_batch_create(aloha_ctx* ctx, const int* views, int n_items, uint32_t* 
  * warp chunk; ctas_per_sm = 0 picks the occupancy limit. */
 int aloha_batch_set_config(aloha_batch* b, int tile_w, int tile_h, int ctas_per_sm);
 int aloha_batch_get_config(const aloha_batch* b, int* tile_w, int* tile_h, int* ctas_per_sm);
+/* Stencil staging of the batch kernel (ALOHA_STAGING_*, as
+ * aloha_set_render_staging). */
+int aloha_batch_set_staging(aloha_batch* b, int stage);
+int aloha_batch_get_staging(const aloha_batch* b, int* stage);
 int aloha_batch_launch(aloha_batch* b, void* stream);
 int aloha_batch_launch_graph(aloha_batch* b, void* stream);
-/* Time every tile shape (`reps` launches each, CUDA events) and keep the
- * fastest; returns its shape and mean milliseconds per launch. */
+/* Time every tile shape with each staging (`reps` launches each, CUDA
+ * events) and keep the fastest; returns its shape and mean milliseconds per
+ * launch (aloha_batch_get_staging gives its staging). */
 int aloha_batch_autotune(aloha_batch* b, void* stream, int reps, int* tile_w, int* tile_h, float* ms);
 int aloha_batch_destroy(aloha_batch* b);
 

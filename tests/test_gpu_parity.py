@@ -140,6 +140,56 @@ def test_render_tiles_bit_exact(gpu_ctx_factory, oracle, tile):
         ctx.set_render_split(3)
 
 
+@pytest.mark.parametrize("tile", [(8, 4), (8, 8), (16, 8), (32, 4)])
+@pytest.mark.parametrize("jitter", [abi.JITTER_HASH, abi.JITTER_CONST])
+def test_staged_stencil_loads_bit_exact(gpu_ctx_factory, oracle, tile, jitter):
+    """The next sample's stencil rows staged in shared memory (cp.async) give
+    the frames and sample counts of the direct loads: several ranks per pixel,
+    empty-space skips between full samples (a staged sample dropped), the
+    camera zoo's grazing and inside views, ragged frames, spp 2."""
+    vol, descs, vox, tf = T.uneven_scene(48)
+    W, H = 70, 42
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=4, jitter_mode=jitter, jitter_value=0.37, spp=2)
+    ctx.set_render_split(abi.SPLIT_PIXELS)
+    ctx.set_render_tile(*tile)
+    ctx.set_render_staging(abi.STAGING_NEXT_SAMPLE)
+    params = dict(jitter_mode=jitter, jitter_value=0.37, spp=2)
+    cams = T.cameras((48, 48, 48), 2, W, H, seed=67) + _camera_zoo((48, 48, 48), W, H, seed=68)[::4]
+    for cam in cams:
+        fb, samples = gpu_frame(ctx, cam, W, H)
+        ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=4, **params)
+        assert_same_fb(fb, ref["fb"])
+        assert samples == ref["samples"]
+    with pytest.raises(abi.AlohaError):
+        ctx.set_render_staging(2)
+
+
+def test_staged_batch_equals_direct_batch(gpu_ctx_factory):
+    torch = pytest.importorskip("torch")
+    vol, descs, vox, tf = T.uneven_scene(64)
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=12)
+    sizes = [(96, 96), (64, 48), (40, 72)]
+    for v, (W, H) in enumerate(sizes):
+        ctx.set_camera(v, *S.orbit_cameras((64, 64, 64), len(sizes), W, H, seed=71)[v])
+        ctx.resize(v, W, H)
+    singles = [ctx.render(v, width=W, height=H) for v, (W, H) in enumerate(sizes)]
+    fbs = [torch.zeros((H, W), dtype=torch.int32, device="cuda") for (W, H) in sizes]
+    b = ctx.batch(list(range(len(sizes))), fbs)
+    for cfg in [(8, 4), (16, 8)]:
+        b.set_staging(abi.STAGING_NEXT_SAMPLE)
+        b.set_config(*cfg)
+        assert b.staging() == abi.STAGING_NEXT_SAMPLE
+        for f in fbs:
+            f.zero_()
+        b.launch_graph()
+        torch.cuda.synchronize()
+        for f, s in zip(fbs, singles):
+            assert_same_fb(f.cpu().numpy().view(np.uint32), s)
+    w, h, ms = b.autotune(reps=1)
+    assert b.staging() in (abi.STAGING_NONE, abi.STAGING_NEXT_SAMPLE) and ms > 0
+    b.close()
+
+
 def _camera_zoo(dims, W, H, seed):
     """Cameras that stress the rank split's screen rectangles: near, inside,
     grazing, far with a narrow field of view, off-centre targets."""

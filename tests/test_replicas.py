@@ -53,13 +53,21 @@ class _FakeBatch:
     def __init__(self):
         self.sweeps = 0
         self.config = None
+        self.stage = 0
 
     def autotune(self, stream=None, reps=2):
         self.sweeps += 1
+        self.stage = 1
         return 32, 4, 1.5
 
     def set_config(self, w, h, c):
         self.config = (w, h)
+
+    def set_staging(self, stage):
+        self.stage = stage
+
+    def staging(self):
+        return self.stage
 
 
 def test_autotune_cache(tmp_path):
@@ -71,5 +79,6 @@ def test_autotune_cache(tmp_path):
     assert first["cached"] is False and b.sweeps == 1
     b2 = _FakeBatch()
     second = autotune.tune(b2, key, path=path)
-    assert second["cached"] is True and b2.sweeps == 0 and b2.config == (32, 4)
+    assert second["cached"] is True and b2.sweeps == 0 and b2.config == (32, 4) and b2.stage == 1
     assert json.load(open(path))[key]["tile_w"] == 32
+    assert json.load(open(path))[key]["staging"] == 1
