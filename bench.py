@@ -59,6 +59,13 @@ def parse():
     ap.add_argument("--adjoint-k", type=int, default=32, help="checkpoint every K samples in the adjoint sections")
     ap.add_argument("--only-adjoint", action="store_true",
                     help="run only the 128^3, 16 x 256^2 forward + adjoint configuration and print its timings")
+    ap.add_argument("--only-batched", action="store_true",
+                    help="run only the uneven batched configuration (--n volume, --batch-big views at 1024^2 and "
+                         "--batch-small at 512^2) and print its timings")
+    ap.add_argument("--batch-big", type=int, default=64)
+    ap.add_argument("--batch-small", type=int, default=32)
+    ap.add_argument("--batch-staging", choices=["tune", "0", "1"], default="tune",
+                    help="with --only-batched: autotune, or fix the stencil staging at the 8x4 tile")
     ap.add_argument("--profile", action="store_true", help="short run for ncu (no baselines, no clocks)")
     return ap.parse_args()
 
@@ -286,6 +293,14 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.only_batched:
+        from aloha_gb300 import scenes as S
+        n = args.n
+        vol = S.blob_field((n, n, n), 64, (n / 16.0, n / 6.4), seed=2001, device=dev)
+        staging = None if args.batch_staging == "tune" else int(args.batch_staging)
+        print(json.dumps(uneven_batched_section(vol, dev, args.batch_big, args.batch_small, staging=staging,
+                                                profile=args.profile)), flush=True)
+        return
     if args.only_adjoint:
         from aloha_gb300 import scenes as S
         if args.adjoint_case == "volume":
@@ -604,11 +619,13 @@ def staging_sweep(b, stream, timed):
     return out
 
 
-def uneven_batched_section(vol, dev, big=64, small=32):
+def uneven_batched_section(vol, dev, big=64, small=32, staging=None, profile=False):
     """The batched configuration: the same 512^3 field in uneven 3x2x2 bricks
     (x cuts 200, 380; y 256; z 300), 64 views at 1024^2 and 32 at 512^2 in one
     graph-captured persistent launch (autotuned), against the same views as
-    plain aloha_render launches."""
+    plain aloha_render launches.  `staging` fixes the stencil staging at the
+    8x4 tile instead of autotuning; `profile` launches the batch once and
+    times nothing (for ncu)."""
     import torch
 
     from aloha_gb300 import abi
@@ -633,7 +650,20 @@ def uneven_batched_section(vol, dev, big=64, small=32):
         ctx.render(v, fbs[-1], stream)
         samples += ctx.stats().samples
     b = ctx.batch(list(range(len(sizes))), fbs)
-    tw, th, _ = b.autotune(stream, reps=1)
+    if staging is None:
+        tw, th, _ = b.autotune(stream, reps=1)
+    else:
+        tw, th = 8, 4
+        b.set_staging(staging)
+        b.set_config(tw, th)
+    if profile:
+        b.launch_graph(stream)
+        torch.cuda.synchronize()
+        chosen = b.staging()
+        b.close()
+        ctx.close()
+        return {"config": f"{n}^3 in {len(descs)} uneven bricks, {big} views at 1024^2 + {small} at 512^2",
+                "tile": [tw, th], "staging": STAGING_NAMES[chosen], "profile": True}
 
     def timed(fn, reps=3):
         for _ in range(2):
