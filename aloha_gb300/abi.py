@@ -37,7 +37,7 @@ EXPORTS = [
     "aloha_batch_set_config", "aloha_batch_get_config", "aloha_batch_launch", "aloha_batch_launch_graph",
     "aloha_batch_autotune", "aloha_batch_destroy", "aloha_render_batch", "aloha_forward", "aloha_backward",
     "aloha_composite_over_noalloc", "aloha_set_render_tile", "aloha_set_render_split", "aloha_set_chunk_order",
-    "aloha_set_render_staging", "aloha_batch_set_staging", "aloha_batch_get_staging",
+    "aloha_set_render_staging", "aloha_batch_set_staging", "aloha_batch_get_staging", "aloha_set_lane_groups",
 ]
 
 
@@ -108,6 +108,7 @@ _SIGS = {
     "aloha_set_render_split": ([P, I], I),
     "aloha_set_chunk_order": ([P, I], I),
     "aloha_set_render_staging": ([P, I], I),
+    "aloha_set_lane_groups": ([P, I], I),
     "aloha_batch_set_staging": ([P, I], I),
     "aloha_batch_get_staging": ([P, ctypes.POINTER(I)], I),
 }
@@ -267,6 +268,11 @@ class Context:
         """STAGING_NONE or STAGING_NEXT_SAMPLE (the next sample's stencil rows
         copied into shared memory with cp.async); frames are bit-identical."""
         self._check(self._lib.aloha_set_render_staging(self.h, int(mode)))
+
+    def set_lane_groups(self, permille: int):
+        """Share (per mille) of a cost-ordered frame's costliest 8x4 chunks rendered
+        with 4 lanes per ray; frames are bit-identical; 0 is off."""
+        self._check(self._lib.aloha_set_lane_groups(self.h, int(permille)))
 
     def set_render_split(self, mode: int):
         """SPLIT_AUTO, SPLIT_PIXELS (one thread per pixel over all ranks) or

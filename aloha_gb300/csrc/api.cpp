@@ -147,6 +147,8 @@ struct aloha_ctx {
   int split_mode = ALOHA_SPLIT_AUTO;
   int staging = ALOHA_STAGING_NONE;  // stencil loads of the single-view render kernel
   int grid_stage = -1;
+  int lane_group_permille = 0;       // share of the cost order rendered by lane groups
+  int grid_blocks_lg = 0, grid_lg_n_tf = -1;
   DeviceBuffer split_images, split_masks, split_items, split_done;
   int split_grid_n_tf = -1, split_grid_blocks = 0;
   int chunk_order_slots = -1;  // slot count of the chunk-order buffer's current layout
@@ -540,9 +542,24 @@ int launch_single(aloha_ctx* c, const FrameArgs& f, int view, cudaStream_t s) {
     CUDA_TRY(c, cudaMemsetAsync(c->work.ptr, 0, sizeof(unsigned int), s));
     CUDA_TRY(c, cudaMemsetAsync(f.counter, 0, sizeof(unsigned long long), s));
   }
+  // lane groups for the costliest chunks (cost order, 8x4, direct loads, frame buffer only)
+  bool lane_groups = false;
+  if (c->lane_group_permille > 0 && order && cw == 8 && ch == 4 && c->staging == ALOHA_STAGING_NONE && f.fb &&
+      !f.rank_images && !f.rank_depth && !f.accum) {
+    b.group_chunks = (int)(((long long)chunks * c->lane_group_permille + 999) / 1000);
+    b.total_tiles = chunks + b.group_chunks * (kLaneGroup - 1);
+    lane_groups = true;
+    if (c->grid_lg_n_tf != c->n_tf) {
+      const int per_sm = render_blocks_per_sm(8, 4, c->n_tf, false, ALOHA_STAGING_NONE, true);
+      if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "render occupancy query failed");
+      c->grid_blocks_lg = per_sm * c->num_sms;
+      c->grid_lg_n_tf = c->n_tf;
+    }
+  }
   const int warps_per_block = kRenderThreads / 32;
-  const int grid = std::max(1, std::min(c->grid_blocks, (b.total_tiles + warps_per_block - 1) / warps_per_block));
-  CUDA_TRY(c, launch_render_warps(b, cw, ch, grid, false, s, c->staging));
+  const int grid = std::max(1, std::min(lane_groups ? c->grid_blocks_lg : c->grid_blocks,
+                                        (b.total_tiles + warps_per_block - 1) / warps_per_block));
+  CUDA_TRY(c, launch_render_warps(b, cw, ch, grid, false, s, c->staging, lane_groups));
   return ALOHA_OK;
 }
 
@@ -995,6 +1012,14 @@ int aloha_set_render_staging(aloha_ctx* c, int mode) {
   if (mode != ALOHA_STAGING_NONE && mode != ALOHA_STAGING_NEXT_SAMPLE)
     return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "staging %d not NONE (0) or NEXT_SAMPLE (1)", mode);
   c->staging = mode;
+  return ALOHA_OK;
+}
+
+int aloha_set_lane_groups(aloha_ctx* c, int permille) {
+  if (!c) return ALOHA_ERR_NULL_POINTER;
+  if (permille < 0 || permille > 1000)
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "lane-group share %d not in [0, 1000] per mille", permille);
+  c->lane_group_permille = permille;
   return ALOHA_OK;
 }
 

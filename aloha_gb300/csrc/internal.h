@@ -83,7 +83,12 @@ struct BatchArgs {
   int total_tiles;           // chunks in the launch
   unsigned int* work_counter;
   const int* chunk_order;    // single view: chunk ids in the order to render them, or null (ring order)
+  int group_chunks;          // single view in cost order: the first group_chunks chunks of chunk_order are
+                             // rendered by lane groups (kLaneGroup lanes per ray), as kLaneGroup items each
 };
+
+// Lanes per ray of the lane-group render (march_brick_group).
+constexpr int kLaneGroup = 4;
 
 // Cost-ordered chunks of one view (schedule.cu): a coarse probe per chunk
 // estimates its cost, and the chunks are sorted stably by cost class, most
@@ -155,8 +160,10 @@ cudaError_t launch_pad_brick(const float* src, int nx, int ny, int nz, float4* d
 // Persistent render launch; `batch` selects the instance tuned for batches.
 constexpr int kSingleRenderBlocks = 5, kBatchRenderBlocks = 7;  // CTAs per SM
 // `stage`: ALOHA_STAGING_NONE or _NEXT_SAMPLE (the stencil loads).
+// `lane_groups`: the instance that renders the first a.group_chunks chunks of
+// the cost order with lane groups (single view, 8x4 chunks, direct loads).
 cudaError_t launch_render_warps(const BatchArgs& a, int chunk_w, int chunk_h, int grid, bool batch, cudaStream_t s,
-                                int stage = ALOHA_STAGING_NONE);
+                                int stage = ALOHA_STAGING_NONE, bool lane_groups = false);
 cudaError_t launch_macrocell_range(const DevBrick& b, float2* out, cudaStream_t s);
 cudaError_t launch_macrocell_empty(const float2* ranges, int count, const int* prefix, int n, uint8_t* empty,
                                    cudaStream_t s);
@@ -165,7 +172,8 @@ inline int macrocells(const DevBrick& b) {
          ((b.n[2] + kMacro - 1) >> kMacroShift);
 }
 // CTAs of the render kernel that fit on one SM for a chunk shape (0 if the shape is unknown).
-int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf, bool batch, int stage = ALOHA_STAGING_NONE);
+int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf, bool batch, int stage = ALOHA_STAGING_NONE,
+                         bool lane_groups = false);
 // `many_ranks` selects the instance tuned for many short (chunk, rank) items.
 constexpr int kManyRankSplitBlocks = 7;  // CTAs per SM
 cudaError_t launch_render_split(const SplitArgs& a, int grid, bool many_ranks, cudaStream_t s);

@@ -138,6 +138,12 @@ __device__ __forceinline__ StencilOut stencil_rows(const float4 r00, const float
   return s;
 }
 
+// kClamp: clamp the indices into the apron.  A march may leave them unclamped
+// when every coordinate it samples lies in [-1/4, n + 1/4] per axis
+// (march_safe): then floor(u - 1/2) >= -1, floor(u) <= n, floor(u - 1/2) <= n - 1,
+// and the extra row floor(u) + 2 is taken only when frac(u) >= 1/2, so it is
+// at most n + 1 -- every index already lies in the apron.
+template <bool kClamp = true>
 __device__ __forceinline__ StencilOut stencil(const float4* __restrict__ base, int sy, int sz, int nx, int ny,
                                               int nz, float ux, float uy, float uz) {
   const float mx = ux - 0.5f, my = uy - 0.5f, mz = uz - 0.5f;
@@ -149,12 +155,12 @@ __device__ __forceinline__ StencilOut stencil(const float4* __restrict__ base, i
   // Indices, clamped into the apron.  Every index the oracle clamps to the
   // edge maps to an apron voxel holding that edge value, so these clamps only
   // keep pathological coordinates in bounds and never change a value.
-  const int ix = min(max((int)fmx, -kApron), nx - 1);
-  const int iy = min(max((int)fmy, -kApron), ny - 1);
-  const int iz = min(max((int)fmz, -kApron), nz - 1);
-  const int cx = min(max((int)fcx, -kApron), nx);
-  const int cy = min(max((int)fcy, -kApron), ny);
-  const int cz = min(max((int)fcz, -kApron), nz);
+  const int ix = kClamp ? min(max((int)fmx, -kApron), nx - 1) : (int)fmx;
+  const int iy = kClamp ? min(max((int)fmy, -kApron), ny - 1) : (int)fmy;
+  const int iz = kClamp ? min(max((int)fmz, -kApron), nz - 1) : (int)fmz;
+  const int cx = kClamp ? min(max((int)fcx, -kApron), nx) : (int)fcx;
+  const int cy = kClamp ? min(max((int)fcy, -kApron), ny) : (int)fcy;
+  const int cz = kClamp ? min(max((int)fcz, -kApron), nz) : (int)fcz;
 
   // X region: x in {ix, ix+1, ix+2}, y in {cy, cy+1}, z in {cz, cz+1}: one
   // quad per (y, z) row.
@@ -336,10 +342,10 @@ struct NoHook {
 
 // integrateBrick (deviceCode.cpp:256-298) over [t0, t1); returns the number
 // of samples taken.
-template <class Hook, class Loads = DirectLoads>
-__device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
-                                                const Ray& r, float t0, float t1, float ils, float dt, float et,
-                                                float4& color, Hook& hook, Loads& loads) {
+template <class Hook, class Loads, bool kClamp>
+__device__ __forceinline__ uint32_t march_brick_loop(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
+                                                     const Ray& r, float t0, float t1, float ils, float dt, float et,
+                                                     float4& color, Hook& hook, Loads& loads) {
   const float4* __restrict__ base = b.base;
   const int sy = b.sy, sz = b.sz, nx = b.n[0], ny = b.n[1], nz = b.n[2];
   const float lox = b.lo[0], loy = b.lo[1], loz = b.lo[2];
@@ -438,7 +444,7 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
     if constexpr (Loads::kStaged)
       s = loads.sample(base, sy, sz, nx, ny, nz, ux, uy, uz, t, t1, dt, r.o, r.d, lox, loy, loz);
     else
-      s = stencil(base, sy, sz, nx, ny, nz, ux, uy, uz);
+      s = stencil<kClamp>(base, sy, sz, nx, ny, nz, ux, uy, uz);
     const float shade = shade_factor(s, r);
     const float4 c = tf_lookup(tf_s, n_tf, nf, s.value);
     composite_step(color, c, shade);
@@ -447,12 +453,163 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
   return n;
 }
 
+// True when every sample coordinate of a brick march over [t0, t1) lies in
+// [-1/4, n + 1/4] per axis, so the stencil needs no index clamps: the brick's
+// space box lies inside its voxel range [lo, lo + n], and the march's rounding
+// margin (the eps of march_brick_loop, a bound on the position error in voxel
+// units) is at most 1/4 voxel.
+__device__ __forceinline__ bool march_safe(const DevBrick& b, const Ray& r, float t1) {
+  const float mag = fmaxf(fmaxf(fabsf(r.o[0]) + fabsf(b.lo[0]), fabsf(r.o[1]) + fabsf(b.lo[1])),
+                          fabsf(r.o[2]) + fabsf(b.lo[2])) + fabsf(t1);
+  bool inside = 2e-6f * mag + 1e-4f <= 0.25f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    inside = inside && b.space_lo[a] >= b.lo[a] && b.space_hi[a] <= b.lo[a] + (float)b.n[a];
+  return inside;
+}
+
+// integrateBrick over [t0, t1) (see march_brick_loop); the loop without index
+// clamps when march_safe holds (the same values, fewer instructions).
+template <class Hook, class Loads = DirectLoads>
+__device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
+                                                const Ray& r, float t0, float t1, float ils, float dt, float et,
+                                                float4& color, Hook& hook, Loads& loads) {
+  if (march_safe(b, r, t1))
+    return march_brick_loop<Hook, Loads, false>(b, tf_s, n_tf, r, t0, t1, ils, dt, et, color, hook, loads);
+  return march_brick_loop<Hook, Loads, true>(b, tf_s, n_tf, r, t0, t1, ils, dt, et, color, hook, loads);
+}
+
 template <class Hook>
 __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
                                                 const Ray& r, float t0, float t1, float ils, float dt, float et,
                                                 float4& color, Hook& hook) {
   DirectLoads direct;
   return march_brick(b, tf_s, n_tf, r, t0, t1, ils, dt, et, color, hook, direct);
+}
+
+// ---- Sample-parallel lane groups ------------------------------------------
+// G lanes of a warp march one ray together: all hold the serial march's state
+// (t, n, colour, t_cell) identically.  One group iteration replaces up to G
+// iterations of march_brick_loop:
+//  1. at the base sample (t, n) the loop test and the macrocell test run as
+//     in the serial loop; an empty macrocell starts the same skip run, taken
+//     identically by every lane;
+//  2. lane j takes sample j of the group, at the t the serial loop reaches by
+//     j more rounded additions of dt, if it lies before t1 and under the
+//     iteration cap; past t_cell it looks up its own macrocell and drops the
+//     sample if that one is empty (the serial loop would skip it; a full
+//     sample of alpha 0 leaves the colour unchanged either way);
+//  3. every lane evaluates its sample (stencil, shading, lookup) at once;
+//  4. the samples are composited in lane order from shuffled values, in every
+//     lane: before sample j the serial loop's head test (t_j < t1, colour
+//     alpha < ET, n < cap) decides whether it and the later ones are taken;
+//     each taken sample adds 1 to n and dt to t.
+// The colour, n and t leave the iteration as the serial loop would leave them
+// after the same samples, bit for bit.  A ray's samples take about G times
+// fewer dependent steps, at the cost of the shuffles and of the samples
+// evaluated past the ray's end.
+struct LaneGroup {
+  int lane;       // index in the group, 0..G-1
+  unsigned mask;  // the group's lanes in the warp
+  int base;       // first lane of the group in the warp
+};
+
+template <int G, bool kClamp>
+__device__ __forceinline__ uint32_t march_brick_group_loop(const DevBrick& b, const float4* __restrict__ tf_s,
+                                                           int n_tf, const Ray& r, float t0, float t1, float ils,
+                                                           float dt, float et, float4& color, const LaneGroup& g) {
+  const float4* __restrict__ base = b.base;
+  const int sy = b.sy, sz = b.sz, nx = b.n[0], ny = b.n[1], nz = b.n[2];
+  const float lox = b.lo[0], loy = b.lo[1], loz = b.lo[2];
+  const float nf = (float)n_tf;
+  const uint32_t cap = march_cap(t0, t1, dt);
+  const uint8_t* __restrict__ empty = b.empty;
+  const int mnx = (nx + kMacro - 1) >> kMacroShift, mny = (ny + kMacro - 1) >> kMacroShift;
+  const float offx = r.o[0] - lox, offy = r.o[1] - loy, offz = r.o[2] - loz;
+  const float idx_ = 1.0f / r.d[0], idy = 1.0f / r.d[1], idz = 1.0f / r.d[2];
+  const float mag = fmaxf(fmaxf(fabsf(r.o[0]) + fabsf(lox), fabsf(r.o[1]) + fabsf(loy)),
+                          fabsf(r.o[2]) + fabsf(loz)) + fabsf(t1);
+  const float eps = 2e-6f * mag + 1e-4f;
+  uint32_t n = 0;
+  float t = first_sample_t(t0, dt, ils);
+  const bool exact = exact_steps(t, t1, dt);
+  const float inv_dt = 1.0f / dt;
+  float t_cell = t0;
+  while (t < t1 && color.w < et && n < cap) {
+    if (empty && !(t < t_cell)) {
+      // the base sample's macrocell, exactly as march_brick_loop
+      const float ux = fmaf(t, r.d[0], r.o[0]) - lox;
+      const float uy = fmaf(t, r.d[1], r.o[1]) - loy;
+      const float uz = fmaf(t, r.d[2], r.o[2]) - loz;
+      const int mx = min(max((int)floorf(ux), 0), nx - 1) >> kMacroShift;
+      const int my = min(max((int)floorf(uy), 0), ny - 1) >> kMacroShift;
+      const int mz = min(max((int)floorf(uz), 0), nz - 1) >> kMacroShift;
+      const float bx = (float)(mx << kMacroShift), by = (float)(my << kMacroShift), bz = (float)(mz << kMacroShift);
+      const float ex = ((r.d[0] > 0.f ? bx + (float)kMacro - eps : bx + eps) - offx) * idx_;
+      const float ey = ((r.d[1] > 0.f ? by + (float)kMacro - eps : by + eps) - offy) * idy;
+      const float ez = ((r.d[2] > 0.f ? bz + (float)kMacro - eps : bz + eps) - offz) * idz;
+      const float tb = fminf(fminf(fminf(ex, ey), ez), t1);
+      if (__ldg(empty + (mz * mny + my) * mnx + mx)) {
+        ++n;
+        t = t + dt;
+        if (exact) {
+          run_steps(t, n, tb, cap, dt, inv_dt, 0xffffffffu);
+          continue;
+        }
+        while (t < tb && n < cap) {
+          ++n;
+          t = t + dt;
+        }
+        continue;
+      }
+      t_cell = tb;
+    }
+    // this lane's sample: the serial loop's t after g.lane more steps
+    float tk = t;
+    for (int j = 0; j < g.lane; ++j) tk = tk + dt;
+    const bool in_range = tk < t1 && n + (uint32_t)g.lane < cap;
+    bool full = in_range;
+    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+    float shade = 0.f;
+    if (in_range) {
+      const float vx = fmaf(tk, r.d[0], r.o[0]) - lox;
+      const float vy = fmaf(tk, r.d[1], r.o[1]) - loy;
+      const float vz = fmaf(tk, r.d[2], r.o[2]) - loz;
+      if (empty && !(tk < t_cell)) {
+        const int mx = min(max((int)floorf(vx), 0), nx - 1) >> kMacroShift;
+        const int my = min(max((int)floorf(vy), 0), ny - 1) >> kMacroShift;
+        const int mz = min(max((int)floorf(vz), 0), nz - 1) >> kMacroShift;
+        full = !__ldg(empty + (mz * mny + my) * mnx + mx);
+      }
+      if (full) {
+        const StencilOut s = stencil<kClamp>(base, sy, sz, nx, ny, nz, vx, vy, vz);
+        shade = shade_factor(s, r);
+        c = tf_lookup(tf_s, n_tf, nf, s.value);
+      }
+    }
+    const unsigned in_mask = __ballot_sync(g.mask, in_range) >> g.base;
+    const unsigned full_mask = __ballot_sync(g.mask, full) >> g.base;
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+      const float cx = __shfl_sync(g.mask, c.x, j, G), cy = __shfl_sync(g.mask, c.y, j, G);
+      const float cz = __shfl_sync(g.mask, c.z, j, G), cw = __shfl_sync(g.mask, c.w, j, G);
+      const float sh = __shfl_sync(g.mask, shade, j, G);
+      if (!((in_mask >> j) & 1u) || !(color.w < et)) break;
+      if ((full_mask >> j) & 1u) composite_step(color, make_float4(cx, cy, cz, cw), sh);
+      ++n;
+      t = t + dt;
+    }
+  }
+  return n;
+}
+
+template <int G>
+__device__ __forceinline__ uint32_t march_brick_group(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
+                                                      const Ray& r, float t0, float t1, float ils, float dt, float et,
+                                                      float4& color, const LaneGroup& g) {
+  if (march_safe(b, r, t1))
+    return march_brick_group_loop<G, false>(b, tf_s, n_tf, r, t0, t1, ils, dt, et, color, g);
+  return march_brick_group_loop<G, true>(b, tf_s, n_tf, r, t0, t1, ils, dt, et, color, g);
 }
 
 __device__ __forceinline__ float saturatef_(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
@@ -490,10 +647,10 @@ __device__ __forceinline__ void load_tf(float4* tf_s, const float4* __restrict__
 // rank's bricks [j0, j1) of the view schedule front to back, spp draws, early
 // termination on the rank's own alpha.  Returns the spp sum of the colours;
 // z = nearest brick entry / max depth, ns = samples taken.
-template <class Loads = DirectLoads>
+template <class Loads = DirectLoads, int G = 1>
 __device__ __forceinline__ float4 march_rank(const FrameArgs& a, const DevView& v, const float4* tf_s, const Ray& ray,
                                              const int* __restrict__ rbricks, int j0, int j1, int pixel, float& z,
-                                             uint32_t& ns, Loads& loads) {
+                                             uint32_t& ns, Loads& loads, const LaneGroup& g = LaneGroup{0, 0u, 0}) {
   float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
   uint32_t draw = 0;
   for (int s = 0; s < a.spp; ++s) {
@@ -507,7 +664,10 @@ __device__ __forceinline__ float4 march_rank(const FrameArgs& a, const DevView& 
       const float tnear = (t0 > tmin ? t0 : 0.0f) + tmin;
       z = fminf(z, tnear / v.max_depth);
       NoHook none;
-      ns += march_brick(b, tf_s, a.n_tf, ray, t0, t1, ils, a.dt, a.et_alpha, color, none, loads);
+      if constexpr (G > 1)
+        ns += march_brick_group<G>(b, tf_s, a.n_tf, ray, t0, t1, ils, a.dt, a.et_alpha, color, g);
+      else
+        ns += march_brick(b, tf_s, a.n_tf, ray, t0, t1, ils, a.dt, a.et_alpha, color, none, loads);
       tmin = t1 + 1e-20f;
       if (!(color.w < a.et_alpha)) break;
     }
@@ -600,9 +760,13 @@ __device__ __forceinline__ bool pixel_in_island(const FrameArgs& a, int W, int x
 // One pixel of one view: every virtual rank marches its bricks and runs
 // renderFrame's output stage; the rank images are blended front to back.
 // Returns the number of samples.
-template <class Loads = DirectLoads>
+// With G > 1 the G lanes of `g` render the pixel together (a lane group);
+// only the group's first lane writes the frame buffer.  The group form has no
+// accumulation buffer and no rank planes (the caller ensures it).
+template <class Loads = DirectLoads, int G = 1>
 __device__ __forceinline__ uint32_t render_pixel(const FrameArgs& a, const DevView& v, const float4* tf_s, int x,
-                                                 int y, uint32_t* fb_out, size_t fb_index, Loads& loads) {
+                                                 int y, uint32_t* fb_out, size_t fb_index, Loads& loads,
+                                                 const LaneGroup& g = LaneGroup{0, 0u, 0}) {
   const int W = v.width, H = v.height;
   const int pixel = x + W * y;
   const size_t npx = (size_t)W * H;
@@ -620,11 +784,12 @@ __device__ __forceinline__ uint32_t render_pixel(const FrameArgs& a, const DevVi
     uint32_t ns = 0;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (in_island)
-      acc = march_rank(a, v, tf_s, ray, rbricks, __ldg(rstart + r), __ldg(rstart + r + 1), pixel, z, ns, loads);
+      acc = march_rank<Loads, G>(a, v, tf_s, ray, rbricks, __ldg(rstart + r), __ldg(rstart + r + 1), pixel, z, ns,
+                                 loads, g);
     blend.add(a.composite_mode, rank_output(a, W, H, r, x, y, pixel, npx, acc, ns, z, a.rank_images, a.rank_depth));
     total += ns;
   }
-  if (fb_out) fb_out[fb_index] = blend.pack(a.composite_mode);
+  if (fb_out && (G == 1 || g.lane == 0)) fb_out[fb_index] = blend.pack(a.composite_mode);
   return total;
 }
 

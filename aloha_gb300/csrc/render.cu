@@ -24,8 +24,12 @@ namespace aloha {
 // resident warps (7 CTAs, 72 registers).
 // STAGE selects the stencil loads: 0 direct, 1 the next sample's rows staged
 // in shared memory with cp.async (StagedLoads; shared memory after the
-// transfer function).
-template <int CW, int CH, int MINB, int STAGE>
+// transfer function).  LG > 1 (single view in cost order, 8x4 chunks, frame
+// buffer only): work positions [0, LG * group_chunks) are the costliest
+// group_chunks chunks, each as LG items of 32 / LG pixels rendered by lane
+// groups of LG lanes per ray; the remaining positions are the other chunks of
+// the cost order, rendered as usual.
+template <int CW, int CH, int MINB, int STAGE, int LG = 1>
 __global__ void __launch_bounds__(kRenderThreads, MINB) render_warps_kernel(BatchArgs b) {
   extern __shared__ float4 tf_s[];
   load_tf(tf_s, b.f.tf, b.f.n_tf);
@@ -58,6 +62,22 @@ __global__ void __launch_bounds__(kRenderThreads, MINB) render_warps_kernel(Batc
     uint32_t* fb = b.fbs ? b.fbs[item] : b.f.fb;
     int ccx, ccy;
     const int cxn = (v.width + CW - 1) / CW;
+    if constexpr (LG > 1) {
+      if (chunk < b.group_chunks * LG) {
+        const int id = __ldg(b.chunk_order + chunk / LG), part = chunk % LG;
+        const int gl = lane % LG, p = part * (32 / LG) + lane / LG;
+        const int x = (id % cxn) * 8 + (p & 7), y = (id / cxn) * 4 + (p >> 3);
+        const LaneGroup g{gl, ((1u << LG) - 1u) << (lane - gl), lane - gl};
+        // the group's lanes share x and y, so they take this branch together
+        if (x < v.width && y < v.height) {
+          const uint32_t ns =
+              render_pixel<Loads, LG>(b.f, v, tf_s, x, y, fb, (size_t)x + (size_t)v.width * y, loads, g);
+          if (gl == 0) n += ns;
+        }
+        continue;
+      }
+      chunk -= b.group_chunks * (LG - 1);  // position in the cost order of the remaining chunks
+    }
     if (b.chunk_order) {
       const int id = __ldg(b.chunk_order + chunk);
       ccx = id % cxn;
@@ -424,7 +444,11 @@ RenderKernel render_kernel_for(int chunk_w, int chunk_h) {
   return nullptr;
 }
 
-RenderKernel render_kernel(int chunk_w, int chunk_h, bool batch, int stage) {
+RenderKernel render_kernel(int chunk_w, int chunk_h, bool batch, int stage, bool lane_groups) {
+  if (lane_groups)
+    return (!batch && stage == ALOHA_STAGING_NONE && chunk_w == 8 && chunk_h == 4)
+               ? render_warps_kernel<8, 4, kSingleRenderBlocks, 0, kLaneGroup>
+               : nullptr;
   if (stage == ALOHA_STAGING_NEXT_SAMPLE)
     return batch ? render_kernel_for<kBatchRenderBlocks, 1>(chunk_w, chunk_h)
                  : render_kernel_for<kSingleRenderBlocks, 1>(chunk_w, chunk_h);
@@ -436,15 +460,16 @@ RenderKernel render_kernel(int chunk_w, int chunk_h, bool batch, int stage) {
 }  // namespace
 
 cudaError_t launch_render_warps(const BatchArgs& b, int chunk_w, int chunk_h, int grid, bool batch, cudaStream_t s,
-                                int stage) {
-  const RenderKernel k = render_kernel(chunk_w, chunk_h, batch, stage);
+                                int stage, bool lane_groups) {
+  if (lane_groups && (!b.chunk_order || b.f.rank_images || b.f.rank_depth || b.f.accum)) return cudaErrorInvalidValue;
+  const RenderKernel k = render_kernel(chunk_w, chunk_h, batch, stage, lane_groups);
   if (!k) return cudaErrorInvalidValue;
   k<<<grid, kRenderThreads, render_smem(b.f.n_tf, stage), s>>>(b);
   return cudaGetLastError();
 }
 
-int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf, bool batch, int stage) {
-  const RenderKernel k = render_kernel(chunk_w, chunk_h, batch, stage);
+int render_blocks_per_sm(int chunk_w, int chunk_h, int n_tf, bool batch, int stage, bool lane_groups) {
+  const RenderKernel k = render_kernel(chunk_w, chunk_h, batch, stage, lane_groups);
   int n = 0;
   if (!k || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kRenderThreads, render_smem(n_tf, stage)) !=
                 cudaSuccess) {

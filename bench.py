@@ -345,18 +345,23 @@ def main():
     # work-division sweep of the single-view render (untimed): the pixel split
     # at three chunk shapes, and the (chunk, rank) split
     none, staged = abi.STAGING_NONE, abi.STAGING_NEXT_SAMPLE
-    schedules = {"pixels 8x4": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_PROBED, none),
-                 "pixels 8x4 staged": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_PROBED, staged),
-                 "pixels 8x4 ring order": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_RING, none),
-                 "pixels 8x8": (abi.SPLIT_PIXELS, 8, 8, abi.CHUNKS_PROBED, none),
-                 "pixels 16x8": (abi.SPLIT_PIXELS, 16, 8, abi.CHUNKS_PROBED, none),
-                 "ranks": (abi.SPLIT_RANKS, 0, 0, abi.CHUNKS_AUTO, none)}
+    # (split, chunk w, h, chunk order, staging, lane-group share per mille)
+    schedules = {"pixels 8x4": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_PROBED, none, 0),
+                 "pixels 8x4 lane groups 1%": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_PROBED, none, 10),
+                 "pixels 8x4 lane groups 4%": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_PROBED, none, 40),
+                 "pixels 8x4 lane groups 15%": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_PROBED, none, 150),
+                 "pixels 8x4 staged": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_PROBED, staged, 0),
+                 "pixels 8x4 ring order": (abi.SPLIT_PIXELS, 8, 4, abi.CHUNKS_RING, none, 0),
+                 "pixels 8x8": (abi.SPLIT_PIXELS, 8, 8, abi.CHUNKS_PROBED, none, 0),
+                 "pixels 16x8": (abi.SPLIT_PIXELS, 16, 8, abi.CHUNKS_PROBED, none, 0),
+                 "ranks": (abi.SPLIT_RANKS, 0, 0, abi.CHUNKS_AUTO, none, 0)}
     sched_ms = {}
-    for name, (split, tw, th, chunks, stage) in schedules.items():
+    for name, (split, tw, th, chunks, stage, lg) in schedules.items():
         ctx.set_render_split(split)
         ctx.set_render_tile(tw, th)
         ctx.set_chunk_order(chunks)
         ctx.set_render_staging(stage)
+        ctx.set_lane_groups(lg)
         probe = mine[:8]
         for ci in probe[:2]:
             ctx.set_camera(0, *cams[ci])
@@ -372,12 +377,14 @@ def main():
             ms += e0.elapsed_time(e1)
         sched_ms[name] = ms / len(probe)
     best = min(sched_ms, key=sched_ms.get)
-    split, tw, th, chunks, stage = schedules[best]
+    split, tw, th, chunks, stage, lg = schedules[best]
     ctx.set_render_split(split)
     ctx.set_render_tile(tw, th)
     ctx.set_chunk_order(chunks)
     ctx.set_render_staging(stage)
-    kernel = "render_split_kernel" if split == abi.SPLIT_RANKS else f"render_warps_kernel<{tw},{th},5,{stage}>"
+    ctx.set_lane_groups(lg)
+    kernel = ("render_split_kernel" if split == abi.SPLIT_RANKS else
+              f"render_warps_kernel<{tw},{th},5,{stage}{',4' if lg else ''}>")
     # our kernels per frame: the render, plus the chunk probe (which also
     # counts the classes), scan and scatter of the cost order, and for the
     # rank split its mask, three scan kernels and emit

@@ -177,6 +177,17 @@ int aloha_set_chunk_order(aloha_ctx* ctx, int mode);
  * reference samples 3D textures, deviceCode.cpp:279-289). */
 int aloha_set_render_staging(aloha_ctx* ctx, int mode);
 
+/* Sample-parallel lane groups for the costliest chunks of a single-view
+ * render: the first `permille` / 1000 of the cost order's 8x4 chunks are
+ * rendered with 4 lanes per ray (each lane evaluates one of 4 consecutive
+ * samples; the samples are composited in order, so frames and sample counts
+ * are bit-identical), which shortens the frame's longest chunks.  Applies to
+ * cost-ordered frames (ALOHA_CHUNKS_PROBED or automatic from 512^2) with the
+ * 8x4 chunk, direct stencil loads and a frame buffer only (not to
+ * aloha_render_partials, accumulation or the rank split).  0 (the default)
+ * is off.  No reference counterpart (one OptiX thread per pixel). */
+int aloha_set_lane_groups(aloha_ctx* ctx, int permille);
+
 /* Render one view into an RGBA8 frame buffer of width*height uint32
  * (Renderer::render, waikikiRenderer.cpp:1015-1080): all virtual ranks march
  * their bricks and their images are composited in one fused kernel.  fb may

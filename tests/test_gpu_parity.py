@@ -164,6 +164,32 @@ def test_staged_stencil_loads_bit_exact(gpu_ctx_factory, oracle, tile, jitter):
         ctx.set_render_staging(2)
 
 
+@pytest.mark.parametrize("permille", [1000, 100])
+@pytest.mark.parametrize("kw", [dict(), dict(jitter_mode=abi.JITTER_CONST, jitter_value=0.37),
+                                dict(dt=0.3, spp=2), dict(dt=0.375, jitter_mode=abi.JITTER_NONE),
+                                dict(et_alpha=2.0)])
+def test_lane_groups_bit_exact(gpu_ctx_factory, oracle, permille, kw):
+    """Costliest chunks rendered with 4 lanes per ray (all of them at 1000 per
+    mille): frames and sample counts equal the oracle's -- inexact step
+    sequences (dt 0.3, 0.375), a constant jitter, spp 2, no early termination,
+    several ranks per pixel, the camera zoo's grazing and inside views, ragged
+    frames."""
+    vol, descs, vox, tf = T.uneven_scene(48)
+    W, H = 70, 42
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=4, **kw)
+    ctx.set_render_split(abi.SPLIT_PIXELS)
+    ctx.set_chunk_order(abi.CHUNKS_PROBED)
+    ctx.set_lane_groups(permille)
+    cams = T.cameras((48, 48, 48), 2, W, H, seed=77) + _camera_zoo((48, 48, 48), W, H, seed=78)[::3]
+    for cam in cams:
+        fb, samples = gpu_frame(ctx, cam, W, H)
+        ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=4, **kw)
+        assert_same_fb(fb, ref["fb"])
+        assert samples == ref["samples"]
+    with pytest.raises(abi.AlohaError):
+        ctx.set_lane_groups(1001)
+
+
 def test_staged_batch_equals_direct_batch(gpu_ctx_factory):
     torch = pytest.importorskip("torch")
     vol, descs, vox, tf = T.uneven_scene(64)
