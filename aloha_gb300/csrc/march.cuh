@@ -138,12 +138,6 @@ __device__ __forceinline__ StencilOut stencil_rows(const float4 r00, const float
   return s;
 }
 
-// kClamp: clamp the indices into the apron.  A march may leave them unclamped
-// when every coordinate it samples lies in [-1/4, n + 1/4] per axis
-// (march_safe): then floor(u - 1/2) >= -1, floor(u) <= n, floor(u - 1/2) <= n - 1,
-// and the extra row floor(u) + 2 is taken only when frac(u) >= 1/2, so it is
-// at most n + 1 -- every index already lies in the apron.
-template <bool kClamp = true>
 __device__ __forceinline__ StencilOut stencil(const float4* __restrict__ base, int sy, int sz, int nx, int ny,
                                               int nz, float ux, float uy, float uz) {
   const float mx = ux - 0.5f, my = uy - 0.5f, mz = uz - 0.5f;
@@ -155,12 +149,12 @@ __device__ __forceinline__ StencilOut stencil(const float4* __restrict__ base, i
   // Indices, clamped into the apron.  Every index the oracle clamps to the
   // edge maps to an apron voxel holding that edge value, so these clamps only
   // keep pathological coordinates in bounds and never change a value.
-  const int ix = kClamp ? min(max((int)fmx, -kApron), nx - 1) : (int)fmx;
-  const int iy = kClamp ? min(max((int)fmy, -kApron), ny - 1) : (int)fmy;
-  const int iz = kClamp ? min(max((int)fmz, -kApron), nz - 1) : (int)fmz;
-  const int cx = kClamp ? min(max((int)fcx, -kApron), nx) : (int)fcx;
-  const int cy = kClamp ? min(max((int)fcy, -kApron), ny) : (int)fcy;
-  const int cz = kClamp ? min(max((int)fcz, -kApron), nz) : (int)fcz;
+  const int ix = min(max((int)fmx, -kApron), nx - 1);
+  const int iy = min(max((int)fmy, -kApron), ny - 1);
+  const int iz = min(max((int)fmz, -kApron), nz - 1);
+  const int cx = min(max((int)fcx, -kApron), nx);
+  const int cy = min(max((int)fcy, -kApron), ny);
+  const int cz = min(max((int)fcz, -kApron), nz);
 
   // X region: x in {ix, ix+1, ix+2}, y in {cy, cy+1}, z in {cz, cz+1}: one
   // quad per (y, z) row.
@@ -342,10 +336,10 @@ struct NoHook {
 
 // integrateBrick (deviceCode.cpp:256-298) over [t0, t1); returns the number
 // of samples taken.
-template <class Hook, class Loads, bool kClamp>
-__device__ __forceinline__ uint32_t march_brick_loop(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
-                                                     const Ray& r, float t0, float t1, float ils, float dt, float et,
-                                                     float4& color, Hook& hook, Loads& loads) {
+template <class Hook, class Loads = DirectLoads>
+__device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
+                                                const Ray& r, float t0, float t1, float ils, float dt, float et,
+                                                float4& color, Hook& hook, Loads& loads) {
   const float4* __restrict__ base = b.base;
   const int sy = b.sy, sz = b.sz, nx = b.n[0], ny = b.n[1], nz = b.n[2];
   const float lox = b.lo[0], loy = b.lo[1], loz = b.lo[2];
@@ -444,39 +438,13 @@ __device__ __forceinline__ uint32_t march_brick_loop(const DevBrick& b, const fl
     if constexpr (Loads::kStaged)
       s = loads.sample(base, sy, sz, nx, ny, nz, ux, uy, uz, t, t1, dt, r.o, r.d, lox, loy, loz);
     else
-      s = stencil<kClamp>(base, sy, sz, nx, ny, nz, ux, uy, uz);
+      s = stencil(base, sy, sz, nx, ny, nz, ux, uy, uz);
     const float shade = shade_factor(s, r);
     const float4 c = tf_lookup(tf_s, n_tf, nf, s.value);
     composite_step(color, c, shade);
     t = t + dt;
   }
   return n;
-}
-
-// True when every sample coordinate of a brick march over [t0, t1) lies in
-// [-1/4, n + 1/4] per axis, so the stencil needs no index clamps: the brick's
-// space box lies inside its voxel range [lo, lo + n], and the march's rounding
-// margin (the eps of march_brick_loop, a bound on the position error in voxel
-// units) is at most 1/4 voxel.
-__device__ __forceinline__ bool march_safe(const DevBrick& b, const Ray& r, float t1) {
-  const float mag = fmaxf(fmaxf(fabsf(r.o[0]) + fabsf(b.lo[0]), fabsf(r.o[1]) + fabsf(b.lo[1])),
-                          fabsf(r.o[2]) + fabsf(b.lo[2])) + fabsf(t1);
-  bool inside = 2e-6f * mag + 1e-4f <= 0.25f;
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-    inside = inside && b.space_lo[a] >= b.lo[a] && b.space_hi[a] <= b.lo[a] + (float)b.n[a];
-  return inside;
-}
-
-// integrateBrick over [t0, t1) (see march_brick_loop); the loop without index
-// clamps when march_safe holds (the same values, fewer instructions).
-template <class Hook, class Loads = DirectLoads>
-__device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
-                                                const Ray& r, float t0, float t1, float ils, float dt, float et,
-                                                float4& color, Hook& hook, Loads& loads) {
-  if (march_safe(b, r, t1))
-    return march_brick_loop<Hook, Loads, false>(b, tf_s, n_tf, r, t0, t1, ils, dt, et, color, hook, loads);
-  return march_brick_loop<Hook, Loads, true>(b, tf_s, n_tf, r, t0, t1, ils, dt, et, color, hook, loads);
 }
 
 template <class Hook>
@@ -490,7 +458,7 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
 // ---- Sample-parallel lane groups ------------------------------------------
 // G lanes of a warp march one ray together: all hold the serial march's state
 // (t, n, colour, t_cell) identically.  One group iteration replaces up to G
-// iterations of march_brick_loop:
+// iterations of march_brick:
 //  1. at the base sample (t, n) the loop test and the macrocell test run as
 //     in the serial loop; an empty macrocell starts the same skip run, taken
 //     identically by every lane;
@@ -514,10 +482,10 @@ struct LaneGroup {
   int base;       // first lane of the group in the warp
 };
 
-template <int G, bool kClamp>
-__device__ __forceinline__ uint32_t march_brick_group_loop(const DevBrick& b, const float4* __restrict__ tf_s,
-                                                           int n_tf, const Ray& r, float t0, float t1, float ils,
-                                                           float dt, float et, float4& color, const LaneGroup& g) {
+template <int G>
+__device__ __forceinline__ uint32_t march_brick_group(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
+                                                      const Ray& r, float t0, float t1, float ils, float dt, float et,
+                                                      float4& color, const LaneGroup& g) {
   const float4* __restrict__ base = b.base;
   const int sy = b.sy, sz = b.sz, nx = b.n[0], ny = b.n[1], nz = b.n[2];
   const float lox = b.lo[0], loy = b.lo[1], loz = b.lo[2];
@@ -537,7 +505,7 @@ __device__ __forceinline__ uint32_t march_brick_group_loop(const DevBrick& b, co
   float t_cell = t0;
   while (t < t1 && color.w < et && n < cap) {
     if (empty && !(t < t_cell)) {
-      // the base sample's macrocell, exactly as march_brick_loop
+      // the base sample's macrocell, exactly as march_brick
       const float ux = fmaf(t, r.d[0], r.o[0]) - lox;
       const float uy = fmaf(t, r.d[1], r.o[1]) - loy;
       const float uz = fmaf(t, r.d[2], r.o[2]) - loz;
@@ -582,7 +550,7 @@ __device__ __forceinline__ uint32_t march_brick_group_loop(const DevBrick& b, co
         full = !__ldg(empty + (mz * mny + my) * mnx + mx);
       }
       if (full) {
-        const StencilOut s = stencil<kClamp>(base, sy, sz, nx, ny, nz, vx, vy, vz);
+        const StencilOut s = stencil(base, sy, sz, nx, ny, nz, vx, vy, vz);
         shade = shade_factor(s, r);
         c = tf_lookup(tf_s, n_tf, nf, s.value);
       }
@@ -603,14 +571,6 @@ __device__ __forceinline__ uint32_t march_brick_group_loop(const DevBrick& b, co
   return n;
 }
 
-template <int G>
-__device__ __forceinline__ uint32_t march_brick_group(const DevBrick& b, const float4* __restrict__ tf_s, int n_tf,
-                                                      const Ray& r, float t0, float t1, float ils, float dt, float et,
-                                                      float4& color, const LaneGroup& g) {
-  if (march_safe(b, r, t1))
-    return march_brick_group_loop<G, false>(b, tf_s, n_tf, r, t0, t1, ils, dt, et, color, g);
-  return march_brick_group_loop<G, true>(b, tf_s, n_tf, r, t0, t1, ils, dt, et, color, g);
-}
 
 __device__ __forceinline__ float saturatef_(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
 
