@@ -525,9 +525,12 @@ def adjoint_section(name, vol, descs, cams, W, H, k, stream, dev):
         for v in range(nv):
             ctx.forward(v, img[v], k, stream)
 
-    def bwd(grad, with_tf=True):
+    def bwd(grad, with_tf=True, with_density=True):
         for v in range(nv):
-            ctx.backward(v, grad[v], dtf if with_tf else None, dden, (0, 0, 0), (n, n, n), stream)
+            if with_density:
+                ctx.backward(v, grad[v], dtf if with_tf else None, dden, (0, 0, 0), (n, n, n), stream)
+            else:
+                ctx.backward(v, grad[v], dtf, None, None, None, stream)
 
     fwd()
     grad = (2.0 * (img - target)).contiguous()
@@ -561,12 +564,26 @@ def adjoint_section(name, vol, descs, cams, W, H, k, stream, dev):
         e[2].record(stream)
         torch.cuda.synchronize()
         den_ms += e[1].elapsed_time(e[2]) / reps
+    # transfer-function gradient only (no shading or stencil adjoint)
+    tf_ms = 0.0
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        e[0].record(stream)
+        fwd()
+        e[1].record(stream)
+        bwd(grad, with_density=False)
+        e[2].record(stream)
+        torch.cuda.synchronize()
+        tf_ms += e[1].elapsed_time(e[2]) / reps
     ctx.close()
     return {"config": name, "views": nv, "image": [W, H], "checkpoint_every": k,
             "fwd_ms_per_view": fwd_ms / nv, "adjoint_ms_per_view": bwd_ms / nv,
             "fwd_plus_adjoint_over_fwd": (fwd_ms + bwd_ms) / fwd_ms,
             "adjoint_density_only_ms_per_view": den_ms / nv,
             "fwd_plus_density_adjoint_over_fwd": (fwd_ms + den_ms) / fwd_ms,
+            "adjoint_tf_only_ms_per_view": tf_ms / nv,
+            "fwd_plus_tf_adjoint_over_fwd": (fwd_ms + tf_ms) / fwd_ms,
+            "samples_per_view": samples / nv,
             "fwd_gsamples_per_s": samples / (fwd_ms * 1e-3) / 1e9,
             "fwd_plus_adjoint_gsamples_per_s": samples / ((fwd_ms + bwd_ms) * 1e-3) / 1e9}
 
