@@ -37,12 +37,17 @@
 // Template parameter R = float gives the parity oracle, R = double the FP64
 // re-render used to state the fp32 error.
 //
-// Parity unpinned: the reference ships no tests, golden images or fixtures,
-// and neither its OptiX build nor its ALOHA_CPU build can be compiled here
-// (owl, fakeOwl, IceT and cuteeOwl are empty submodules; MPI, Qt and OptiX are
-// absent).  The restatement is checked against closed forms derived from the
-// reference's arithmetic (tests/test_oracle.py) and its FP64 adjoint against
-// central differences; tests/golden/ holds regression vectors of this oracle.
+// Pinned to the reference: the reference ships no tests, golden images or
+// fixtures, and neither its OptiX build nor its ALOHA_CPU build can be
+// compiled here (owl, fakeOwl, IceT and cuteeOwl are empty submodules; MPI,
+// Qt and OptiX are absent).  Its hot-path sources do compile on their own:
+// ref_harness.cpp runs deviceCode.cpp (unchanged), the Partitioner of
+// waikikiRenderer.cpp and the chopSuey tool on the CPU against the stand-ins
+// in ref_shim/, and tests/test_reference_pin.py compares this restatement
+// with them.  Closed forms derived from the reference's arithmetic
+// (tests/test_oracle.py) and central differences of the FP64 adjoint check it
+// further; tests/golden/ holds regression vectors of this oracle and frames of
+// the reference build.
 #pragma once
 
 #include <algorithm>
