@@ -265,8 +265,8 @@ def reference_arm(args):
     line = {"metric": METRIC, "value": g, "unit": "Gsamples/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": dict(workload_config(args, len(cams), args.gpus),
-                           step=f"one 16-row band of one view (8 bands per view, every H/8 rows)"),
+            "config": workload_config(args, len(cams), args.gpus),
+            "step": "one 16-row band of one view (8 bands per view, every H/8 rows)",
             "cpu_baseline": {"value": g, "unit": "Gsamples/s", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} steps x {rows_per_step} rows x {W} pixels"},
             "e2e": {"value": g, "unit": "Gsamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

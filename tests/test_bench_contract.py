@@ -37,6 +37,11 @@ def test_reference_arm_prints_the_contract_line():
     assert d["steps"] == 3 and d["warmup"] == 3 and d["n_gpus"] == 1
     assert d["config"]["volume"] == [64, 64, 64] and d["config"]["image"] == [64, 64]
     assert "64^3" in d["config"]["workload"]
+    # the same config object as the GPU arm's, so the two lines compare as one workload
+    sys.path.insert(0, ROOT)
+    import bench
+    args = type("A", (), {"n": 64, "size": 64})()
+    assert d["config"] == bench.workload_config(args, 4, 1)
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     e2e = d["e2e"]
