@@ -38,6 +38,7 @@ EXPORTS = [
     "aloha_batch_autotune", "aloha_batch_destroy", "aloha_render_batch", "aloha_forward", "aloha_backward",
     "aloha_composite_over_noalloc", "aloha_set_render_tile", "aloha_set_render_split", "aloha_set_chunk_order",
     "aloha_set_render_staging", "aloha_batch_set_staging", "aloha_batch_get_staging", "aloha_set_lane_groups",
+    "aloha_backward_views",
 ]
 
 
@@ -103,6 +104,7 @@ _SIGS = {
     "aloha_render_batch": ([P, P, I, ctypes.POINTER(P), P], I),
     "aloha_forward": ([P, I, P, I, P], I),
     "aloha_backward": ([P, I, P, P, P, P, P, P], I),
+    "aloha_backward_views": ([P, I, P, P, P, P, P, P, P], I),
     "aloha_composite_over_noalloc": ([P, P, I, I, I, I, P, P], I),
     "aloha_set_render_tile": ([P, I, I], I),
     "aloha_set_render_split": ([P, I], I),
@@ -312,6 +314,19 @@ class Context:
         dims = None if grid_dims is None else np.ascontiguousarray(grid_dims, dtype=np.int32)
         self._check(self._lib.aloha_backward(self.h, view, _addr(dl_drgba), _addr(dl_dtf), _addr(dl_ddensity),
                                              _addr(lo), _addr(dims), _stream(stream)))
+
+    def backward_views(self, views, dl_drgba, dl_dtf, dl_ddensity, grid_lo, grid_dims, stream=None):
+        """backward() of several views, summed: dl_drgba[i] belongs to views[i].  One
+        accumulation buffer and one fold for all of them."""
+        n = len(views)
+        if len(dl_drgba) != n:
+            raise ValueError("one dL/dRGBA per view")
+        v = np.ascontiguousarray(views, dtype=np.int32)
+        ptrs = (P * n)(*[_addr(g) for g in dl_drgba])
+        lo = None if grid_lo is None else np.ascontiguousarray(grid_lo, dtype=np.int32)
+        dims = None if grid_dims is None else np.ascontiguousarray(grid_dims, dtype=np.int32)
+        self._check(self._lib.aloha_backward_views(self.h, n, _addr(v), ptrs, _addr(dl_dtf), _addr(dl_ddensity),
+                                                   _addr(lo), _addr(dims), _stream(stream)))
 
     def stats(self) -> Stats:
         s = Stats()

@@ -119,8 +119,13 @@ class _Render(torch.autograd.Function):
         stream = torch.cuda.current_stream()
         nz, ny, nx = ctx.density_shape
         lo, dims = ((0, 0, 0), (nx, ny, nz)) if want_density else (None, None)
+        # all views in one call: one accumulation buffer, cleared and folded once.
+        # A view listed twice rendered the same image twice from its last
+        # checkpoints, so its output gradients are summed first.
+        per_view: dict[int, torch.Tensor] = {}
         for i, v in enumerate(ctx.views):
-            r.ctx.backward(v, grad[i], dtf, dden, lo, dims, stream)
+            per_view[v] = grad[i] if v not in per_view else per_view[v] + grad[i]
+        r.ctx.backward_views(list(per_view), list(per_view.values()), dtf, dden, lo, dims, stream)
         return dtf, dden, None, None, None
 
 

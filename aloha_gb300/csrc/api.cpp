@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <new>
 #include <string>
@@ -1235,6 +1236,115 @@ TrainArgs train_args(aloha_ctx* c, TrainState& t) {
   return a;
 }
 
+// The backward of several views into one pair of gradients: the views'
+// overflow flags are read with one host wait, their kernels accumulate into
+// one x-quad buffer, and that buffer is cleared and folded into the density
+// grid once.
+int backward_views(aloha_ctx* c, int n_views, const int* view_ids, const float* const* dl_drgba, float* dl_dtf,
+                   float* dl_ddensity, const int* grid_lo, const int* grid_dims, void* stream) {
+  if (!c) return ALOHA_ERR_NULL_POINTER;
+  if (n_views < 1) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "no views");
+  if (!view_ids || !dl_drgba) return c->fail(ALOHA_ERR_NULL_POINTER, "no view list");
+  if (!dl_dtf && !dl_ddensity) return c->fail(ALOHA_ERR_NULL_POINTER, "neither dl_dtf nor dl_ddensity given");
+  if (dl_ddensity && (!grid_lo || !grid_dims)) return c->fail(ALOHA_ERR_NULL_POINTER, "dl_ddensity needs its grid");
+  for (int i = 0; i < n_views; ++i) {
+    const int view = view_ids[i];
+    if (view < 0 || view >= (int)c->views.size()) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "view %d", view);
+    if (!dl_drgba[i]) return c->fail(ALOHA_ERR_NULL_POINTER, "no dL/dRGBA for view %d", view);
+    for (int j = 0; j < i; ++j)
+      if (view_ids[j] == view) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "view %d given twice", view);
+  }
+  int rc = check_trainable(c);
+  if (rc) return rc;
+  for (int i = 0; i < n_views; ++i)
+    if (!c->views[view_ids[i]].train.valid)
+      return c->fail(ALOHA_ERR_NOT_READY, "view %d has no forward checkpoints for the current scene and camera",
+                     view_ids[i]);
+  const bool with_density = dl_ddensity != nullptr;
+  size_t grid_elems = 0;
+  std::vector<int4> origin(with_density ? c->descs.size() : 0);
+  if (with_density) {
+    for (int a = 0; a < 3; ++a)
+      if (grid_dims[a] < 1) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "grid dims must be positive");
+    grid_elems = (size_t)grid_dims[0] * grid_dims[1] * grid_dims[2];
+  }
+  for (size_t b = 0; b < origin.size(); ++b) {
+    const aloha_brick_desc& d = c->descs[b];
+    for (int a = 0; a < 3; ++a)
+      if (d.voxel_lo[a] < grid_lo[a] || d.voxel_hi[a] > grid_lo[a] + grid_dims[a])
+        return c->fail(ALOHA_ERR_OUT_OF_RANGE, "brick %zu's voxel range leaves the gradient grid", b);
+    origin[b] = make_int4(d.voxel_lo[0] - grid_lo[0], d.voxel_lo[1] - grid_lo[1], d.voxel_lo[2] - grid_lo[2], 0);
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  {
+    // every view's overflow flag, read with one wait
+    std::vector<int> overflow(n_views, 0);
+    for (int i = 0; i < n_views; ++i)
+      CUDA_TRY(c, cudaMemcpyAsync(&overflow[i], c->views[view_ids[i]].train.overflow, sizeof(int),
+                                  cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(c, cudaStreamSynchronize(s));
+    for (int i = 0; i < n_views; ++i)
+      if (overflow[i])
+        return c->fail(ALOHA_ERR_OUT_OF_RANGE, "a ray of view %d needed more checkpoints than reserved", view_ids[i]);
+  }
+  const size_t tf_bytes = (size_t)c->n_tf * 4 * sizeof(float), g_bytes = grid_elems * sizeof(float);
+  const bool h_tf = dl_dtf && !is_device_pointer(dl_dtf), h_grid = with_density && !is_device_pointer(dl_ddensity);
+  // device staging for host arguments, in one block: each host dL/dRGBA, dL/dtf, dL/ddensity, origins
+  std::vector<size_t> off_dl(n_views, SIZE_MAX);
+  size_t off = 0;
+  for (int i = 0; i < n_views; ++i)
+    if (!is_device_pointer(dl_drgba[i])) {
+      off_dl[i] = off;
+      off += c->views[view_ids[i]].train.npx * sizeof(float4);
+    }
+  const bool h_dl = off > 0;
+  const size_t off_tf = off;
+  const size_t off_grid = off_tf + (h_tf ? tf_bytes : 0);
+  const size_t off_org = (off_grid + (h_grid ? g_bytes : 0) + 15) & ~(size_t)15;
+  CUDA_TRY(c, c->staging_out.ensure(off_org + origin.size() * sizeof(int4)));
+  char* st = static_cast<char*>(c->staging_out.ptr);
+  float* dtf = h_tf ? reinterpret_cast<float*>(st + off_tf) : dl_dtf;
+  float* grid_out = h_grid ? reinterpret_cast<float*>(st + off_grid) : dl_ddensity;
+  float4* dgrid4 = nullptr;
+  if (with_density) {
+    // the kernels accumulate into x-quads (vector atomics), folded into the grid afterwards
+    CUDA_TRY(c, c->grad4.ensure(grid_elems * sizeof(float4)));
+    dgrid4 = static_cast<float4*>(c->grad4.ptr);
+    CUDA_TRY(c, cudaMemsetAsync(dgrid4, 0, grid_elems * sizeof(float4), s));
+  }
+  for (int i = 0; i < n_views; ++i)
+    if (off_dl[i] != SIZE_MAX)
+      CUDA_TRY(c, cudaMemcpyAsync(st + off_dl[i], dl_drgba[i], c->views[view_ids[i]].train.npx * sizeof(float4),
+                                  cudaMemcpyHostToDevice, s));
+  if (h_tf) CUDA_TRY(c, cudaMemcpyAsync(dtf, dl_dtf, tf_bytes, cudaMemcpyHostToDevice, s));
+  if (h_grid) CUDA_TRY(c, cudaMemcpyAsync(grid_out, dl_ddensity, g_bytes, cudaMemcpyHostToDevice, s));
+  if (with_density)
+    CUDA_TRY(c, cudaMemcpyAsync(st + off_org, origin.data(), origin.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  const int per_sm = backward_blocks_per_sm(c->n_tf);
+  if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "backward occupancy query failed");
+  CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
+  for (int i = 0; i < n_views; ++i) {
+    TrainState& t = c->views[view_ids[i]].train;
+    TrainArgs a = train_args(c, t);
+    a.dl_drgba = off_dl[i] != SIZE_MAX ? reinterpret_cast<const float4*>(st + off_dl[i])
+                                       : reinterpret_cast<const float4*>(dl_drgba[i]);
+    a.dtf = dtf;
+    a.dgrid4 = dgrid4;
+    a.brick_grid_origin = reinterpret_cast<const int4*>(st + off_org);
+    if (with_density)
+      for (int k = 0; k < 3; ++k) a.grid_dims[k] = grid_dims[k];
+    CUDA_TRY(c, cudaMemsetAsync(a.work_count + 2, 0, sizeof(unsigned), s));  // the backward's grab counter
+    CUDA_TRY(c, launch_backward(a, view_ids[i], c->num_sms * per_sm, s));
+  }
+  if (with_density) CUDA_TRY(c, launch_fold_quads(dgrid4, grid_out, grid_dims, s));
+  c->samples_valid = true;
+  if (h_tf) CUDA_TRY(c, cudaMemcpyAsync(dl_dtf, dtf, tf_bytes, cudaMemcpyDeviceToHost, s));
+  if (h_grid) CUDA_TRY(c, cudaMemcpyAsync(dl_ddensity, grid_out, g_bytes, cudaMemcpyDeviceToHost, s));
+  if (h_dl || h_tf || h_grid) CUDA_TRY(c, cudaStreamSynchronize(s));
+  return ALOHA_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1296,73 +1406,12 @@ int aloha_forward(aloha_ctx* c, int view, float* rgba, int checkpoint_every, voi
 int aloha_backward(aloha_ctx* c, int view, const float* dl_drgba, float* dl_dtf, float* dl_ddensity,
                    const int* grid_lo, const int* grid_dims, void* stream) {
   if (!c || !dl_drgba) return ALOHA_ERR_NULL_POINTER;
-  if (!dl_dtf && !dl_ddensity) return c->fail(ALOHA_ERR_NULL_POINTER, "neither dl_dtf nor dl_ddensity given");
-  if (dl_ddensity && (!grid_lo || !grid_dims)) return c->fail(ALOHA_ERR_NULL_POINTER, "dl_ddensity needs its grid");
-  if (view < 0 || view >= (int)c->views.size()) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "view %d", view);
-  int rc = check_trainable(c);
-  if (rc) return rc;
-  ViewState& v = c->views[view];
-  TrainState& t = v.train;
-  if (!t.valid)
-    return c->fail(ALOHA_ERR_NOT_READY, "view %d has no forward checkpoints for the current scene and camera", view);
-  const bool with_density = dl_ddensity != nullptr;
-  size_t grid_elems = 0;
-  std::vector<int4> origin(with_density ? c->descs.size() : 0);
-  if (with_density) {
-    for (int a = 0; a < 3; ++a)
-      if (grid_dims[a] < 1) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "grid dims must be positive");
-    grid_elems = (size_t)grid_dims[0] * grid_dims[1] * grid_dims[2];
-  }
-  for (size_t b = 0; b < origin.size(); ++b) {
-    const aloha_brick_desc& d = c->descs[b];
-    for (int a = 0; a < 3; ++a)
-      if (d.voxel_lo[a] < grid_lo[a] || d.voxel_hi[a] > grid_lo[a] + grid_dims[a])
-        return c->fail(ALOHA_ERR_OUT_OF_RANGE, "brick %zu's voxel range leaves the gradient grid", b);
-    origin[b] = make_int4(d.voxel_lo[0] - grid_lo[0], d.voxel_lo[1] - grid_lo[1], d.voxel_lo[2] - grid_lo[2], 0);
-  }
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  CUDA_TRY(c, cudaSetDevice(c->device));
-  int overflow = 0;
-  CUDA_TRY(c, cudaMemcpyAsync(&overflow, t.overflow, sizeof(int), cudaMemcpyDeviceToHost, s));
-  CUDA_TRY(c, cudaStreamSynchronize(s));
-  if (overflow) return c->fail(ALOHA_ERR_OUT_OF_RANGE, "a ray needed more checkpoints than reserved");
-  const size_t npx = t.npx, tf_bytes = (size_t)c->n_tf * 4 * sizeof(float), g_bytes = grid_elems * sizeof(float);
-  const bool h_dl = !is_device_pointer(dl_drgba), h_tf = dl_dtf && !is_device_pointer(dl_dtf),
-             h_grid = with_density && !is_device_pointer(dl_ddensity);
-  // device staging for host arguments, in one block: dL/dRGBA, dL/dtf, dL/ddensity, origins
-  const size_t off_tf = h_dl ? npx * sizeof(float4) : 0;
-  const size_t off_grid = off_tf + (h_tf ? tf_bytes : 0);
-  const size_t off_org = (off_grid + (h_grid ? g_bytes : 0) + 15) & ~(size_t)15;
-  CUDA_TRY(c, c->staging_out.ensure(off_org + origin.size() * sizeof(int4)));
-  char* st = static_cast<char*>(c->staging_out.ptr);
-  TrainArgs a = train_args(c, t);
-  a.dl_drgba = h_dl ? reinterpret_cast<const float4*>(st) : reinterpret_cast<const float4*>(dl_drgba);
-  a.dtf = h_tf ? reinterpret_cast<float*>(st + off_tf) : dl_dtf;
-  float* grid_out = h_grid ? reinterpret_cast<float*>(st + off_grid) : dl_ddensity;
-  a.brick_grid_origin = reinterpret_cast<const int4*>(st + off_org);
-  if (with_density) {
-    for (int k = 0; k < 3; ++k) a.grid_dims[k] = grid_dims[k];
-    // the kernel accumulates into x-quads (vector atomics), folded into the grid afterwards
-    CUDA_TRY(c, c->grad4.ensure(grid_elems * sizeof(float4)));
-    a.dgrid4 = static_cast<float4*>(c->grad4.ptr);
-    CUDA_TRY(c, cudaMemsetAsync(a.dgrid4, 0, grid_elems * sizeof(float4), s));
-  }
-  if (h_dl) CUDA_TRY(c, cudaMemcpyAsync(st, dl_drgba, npx * sizeof(float4), cudaMemcpyHostToDevice, s));
-  if (h_tf) CUDA_TRY(c, cudaMemcpyAsync(a.dtf, dl_dtf, tf_bytes, cudaMemcpyHostToDevice, s));
-  if (h_grid) CUDA_TRY(c, cudaMemcpyAsync(grid_out, dl_ddensity, g_bytes, cudaMemcpyHostToDevice, s));
-  if (with_density)
-    CUDA_TRY(c, cudaMemcpyAsync(st + off_org, origin.data(), origin.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
-  const int per_sm = backward_blocks_per_sm(c->n_tf);
-  if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "backward occupancy query failed");
-  CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
-  CUDA_TRY(c, cudaMemsetAsync(a.work_count + 2, 0, sizeof(unsigned), s));  // the backward's grab counter
-  CUDA_TRY(c, launch_backward(a, view, c->num_sms * per_sm, s));
-  if (with_density) CUDA_TRY(c, launch_fold_quads(a.dgrid4, grid_out, grid_dims, s));
-  c->samples_valid = true;
-  if (h_tf) CUDA_TRY(c, cudaMemcpyAsync(dl_dtf, a.dtf, tf_bytes, cudaMemcpyDeviceToHost, s));
-  if (h_grid) CUDA_TRY(c, cudaMemcpyAsync(dl_ddensity, grid_out, g_bytes, cudaMemcpyDeviceToHost, s));
-  if (h_dl || h_tf || h_grid) CUDA_TRY(c, cudaStreamSynchronize(s));
-  return ALOHA_OK;
+  return backward_views(c, 1, &view, &dl_drgba, dl_dtf, dl_ddensity, grid_lo, grid_dims, stream);
+}
+
+int aloha_backward_views(aloha_ctx* c, int n_views, const int* views, const float* const* dl_drgba, float* dl_dtf,
+                         float* dl_ddensity, const int* grid_lo, const int* grid_dims, void* stream) {
+  return backward_views(c, n_views, views, dl_drgba, dl_dtf, dl_ddensity, grid_lo, grid_dims, stream);
 }
 
 }  // extern "C"

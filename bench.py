@@ -525,7 +525,12 @@ def adjoint_section(name, vol, descs, cams, W, H, k, stream, dev):
         for v in range(nv):
             ctx.forward(v, img[v], k, stream)
 
-    def bwd(grad, with_tf=True, with_density=True):
+    def bwd(grad, with_tf=True, with_density=True, summed=False):
+        if summed:  # all views in one aloha_backward_views call
+            ctx.backward_views(list(range(nv)), [grad[v] for v in range(nv)], dtf if with_tf else None,
+                               dden if with_density else None, (0, 0, 0) if with_density else None,
+                               (n, n, n) if with_density else None, stream)
+            return
         for v in range(nv):
             if with_density:
                 ctx.backward(v, grad[v], dtf if with_tf else None, dden, (0, 0, 0), (n, n, n), stream)
@@ -575,6 +580,22 @@ def adjoint_section(name, vol, descs, cams, W, H, k, stream, dev):
         e[2].record(stream)
         torch.cuda.synchronize()
         tf_ms += e[1].elapsed_time(e[2]) / reps
+    # the views' gradients summed by one aloha_backward_views call (one
+    # accumulation buffer cleared and folded once, one host wait)
+    sum_ms, sum_den_ms = 0.0, 0.0
+    for _ in range(reps):
+        for with_tf in (True, False):
+            torch.cuda.synchronize()
+            e[0].record(stream)
+            fwd()
+            e[1].record(stream)
+            bwd(grad, with_tf=with_tf, summed=True)
+            e[2].record(stream)
+            torch.cuda.synchronize()
+            if with_tf:
+                sum_ms += e[1].elapsed_time(e[2]) / reps
+            else:
+                sum_den_ms += e[1].elapsed_time(e[2]) / reps
     ctx.close()
     return {"config": name, "views": nv, "image": [W, H], "checkpoint_every": k,
             "fwd_ms_per_view": fwd_ms / nv, "adjoint_ms_per_view": bwd_ms / nv,
@@ -583,6 +604,8 @@ def adjoint_section(name, vol, descs, cams, W, H, k, stream, dev):
             "fwd_plus_density_adjoint_over_fwd": (fwd_ms + den_ms) / fwd_ms,
             "adjoint_tf_only_ms_per_view": tf_ms / nv,
             "fwd_plus_tf_adjoint_over_fwd": (fwd_ms + tf_ms) / fwd_ms,
+            "adjoint_views_summed_ms_per_view": sum_ms / nv,
+            "adjoint_views_summed_density_only_ms_per_view": sum_den_ms / nv,
             "samples_per_view": samples / nv,
             "fwd_gsamples_per_s": samples / (fwd_ms * 1e-3) / 1e9,
             "fwd_plus_adjoint_gsamples_per_s": samples / ((fwd_ms + bwd_ms) * 1e-3) / 1e9}

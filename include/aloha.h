@@ -290,6 +290,19 @@ int aloha_forward(aloha_ctx* ctx, int view, float* rgba, int checkpoint_every, v
 int aloha_backward(aloha_ctx* ctx, int view, const float* dl_drgba, float* dl_dtf, float* dl_ddensity,
                    const int* grid_lo, const int* grid_dims, void* stream);
 
+/* aloha_backward of several views, summed: dl_dtf and dl_ddensity receive the
+ * sum over views[0..n_views) of each view's gradient, with dl_drgba[i] the
+ * dL/dRGBA of views[i] (each view at most once, each with a current
+ * aloha_forward).  Same arguments and rules as aloha_backward otherwise.  The
+ * views' replays accumulate into one device buffer that is cleared and folded
+ * into the density grid once, and their checkpoint-overflow flags are read
+ * with one host wait, so n views cost less than n calls of aloha_backward.
+ * The sum is taken in a different order than n calls would take it (float
+ * atomics), so results agree with those calls to rounding. */
+int aloha_backward_views(aloha_ctx* ctx, int n_views, const int* views, const float* const* dl_drgba,
+                         float* dl_dtf, float* dl_ddensity, const int* grid_lo, const int* grid_dims,
+                         void* stream);
+
 #ifdef __cplusplus
 }
 #endif

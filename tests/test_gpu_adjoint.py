@@ -302,6 +302,71 @@ def test_tf_only_backward(gpu_ctx_factory, oracle, bricks):
     assert e.value.code == abi.ERR_NULL_POINTER
 
 
+@pytest.mark.parametrize("where", ["host", "device"])
+def test_backward_views_is_the_sum(gpu_ctx_factory, oracle, where):
+    """aloha_backward_views over three views (of different sizes) equals the
+    sum of three aloha_backward calls up to the order of the atomic adds, and
+    the FP64 oracle's sum; it accumulates (+=) into what the buffers hold."""
+    torch = pytest.importorskip("torch")
+    n = 48
+    vol, descs, vox = density_scene(n, seed=17, bricks=8)
+    tf = S.ramp_tf()
+    ctx = setup(gpu_ctx_factory, descs, vox, tf)
+    rng = np.random.default_rng(71)
+    sizes = [(80, 72), (64, 64), (96, 40)]
+    views, dls = [0, 2, 1], []
+    ref_tf = np.zeros((tf.shape[0], 4))
+    ref_den = np.zeros((n, n, n))
+    cams = T.cameras((n, n, n), 3, 80, 80, seed=43)
+    for v in views:
+        W, H = sizes[v]
+        ctx.set_camera(v, *cams[v])
+        ctx.resize(v, W, H)
+        ctx.forward(v, np.zeros((H, W, 4), np.float32), 32)
+        dl = rng.uniform(-1, 1, (H, W, 4)).astype(np.float32)
+        dls.append(dl)
+        r = oracle.adjoint(descs, vox, tf, oracle.make_camera(*cams[v]), W, H, dl, (0, 0, 0), (n, n, n))
+        ref_tf += r["dtf"]
+        ref_den += r["ddensity"]
+    one_tf = np.zeros((tf.shape[0], 4), np.float32)
+    one_den = np.zeros((n, n, n), np.float32)
+    for v, dl in zip(views, dls):
+        ctx.backward(v, dl, one_tf, one_den, (0, 0, 0), (n, n, n))
+    start_tf = rng.uniform(-1, 1, (tf.shape[0], 4)).astype(np.float32)
+    start_den = rng.uniform(-1, 1, (n, n, n)).astype(np.float32)
+    if where == "host":
+        many_tf, many_den, dl_in = start_tf.copy(), start_den.copy(), dls
+    else:
+        many_tf, many_den = torch.from_numpy(start_tf).cuda(), torch.from_numpy(start_den).cuda()
+        dl_in = [torch.from_numpy(d).cuda() for d in dls]
+    ctx.backward_views(views, dl_in, many_tf, many_den, (0, 0, 0), (n, n, n))
+    if where == "device":
+        torch.cuda.synchronize()
+        many_tf, many_den = many_tf.cpu().numpy(), many_den.cpu().numpy()
+    many_tf -= start_tf
+    many_den -= start_den
+    # three views of eight bricks: the float32 sums of the single calls sit
+    # near 1e-3 of FP64 on this scene, and the summed call must sit with them
+    for got_tf, got_den in ((one_tf, one_den), (many_tf, many_den)):
+        assert rel_err(got_tf, ref_tf) < 2e-3
+        assert rel_err(got_den, ref_den) < 2e-3
+    np.testing.assert_allclose(many_tf, one_tf, rtol=1e-4, atol=1e-5 * float(np.abs(one_tf).max()))
+    np.testing.assert_allclose(many_den, one_den, rtol=1e-4, atol=1e-5 * float(np.abs(one_den).max()))
+    # the transfer-function-only form, and the argument checks
+    only_tf = np.zeros((tf.shape[0], 4), np.float32)
+    ctx.backward_views(views, dls, only_tf, None, None, None)
+    np.testing.assert_allclose(only_tf, one_tf, rtol=1e-4, atol=1e-5 * float(np.abs(one_tf).max()))
+    for bad, code in [(([0, 0], dls[:2]), abi.ERR_INVALID_ARGUMENT), (([], []), abi.ERR_INVALID_ARGUMENT),
+                      (([0, 5], dls[:2]), abi.ERR_OUT_OF_RANGE)]:
+        with pytest.raises(abi.AlohaError) as e:
+            ctx.backward_views(*bad, only_tf, None, None, None)
+        assert e.value.code == code
+    ctx.set_camera(2, *cams[2])  # view 2's checkpoints are stale now
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.backward_views(views, dls, only_tf, None, None, None)
+    assert e.value.code == abi.ERR_NOT_READY
+
+
 def test_autograd_gradient_flags_and_uploads(gpu_ctx_factory):
     """The binding computes only the gradients autograd asks for, and uploads
     the bricks again only when the density tensor changed."""
