@@ -11,8 +11,10 @@
 //   * the array is a file-scope __device__ array of kNoAllocMaxRanks ints
 //     (16 KB); every GPU that loads the library holds it until exit;
 //   * its device address is looked up with cudaGetSymbolAddress once per
-//     device, on the first call made with that device current, so that first
-//     call should come before any stream capture;
+//     device, on the first call made with that device current;
+//   * the call cannot be recorded into a CUDA graph (its order copy is from
+//     pageable memory): on a capturing stream it returns
+//     ALOHA_ERR_UNSUPPORTED without touching the stream;
 //   * every call on a device shares the one array and overwrites the first
 //     n_ranks entries, so calls whose copies or kernels overlap on the GPU
 //     race; issue them on one stream or wait in between;
@@ -84,9 +86,20 @@ extern "C" int aloha_composite_over_noalloc(const float* rank_images, const int*
   std::memcpy(snapshot, order, sizeof(int) * (size_t)n_ranks);
   for (int k = 0; k < n_ranks; ++k)
     if (snapshot[k] < 0 || snapshot[k] >= n_ranks) return ALOHA_ERR_OUT_OF_RANGE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  {
+    // The snapshot copy is from pageable memory, which a stream capture
+    // cannot record; refuse before touching the stream, so that the caller's
+    // capture stays valid.
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+      cudaGetLastError();
+      return ALOHA_ERR_UNSUPPORTED;
+    }
+    if (cs != cudaStreamCaptureStatusNone) return ALOHA_ERR_UNSUPPORTED;
+  }
   int* d_order = nullptr;
   if (order_scratch(&d_order) != cudaSuccess) return ALOHA_ERR_CUDA;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   // pageable source: staged by the runtime before the call returns
   if (cudaMemcpyAsync(d_order, snapshot, sizeof(int) * (size_t)n_ranks, cudaMemcpyHostToDevice, s) != cudaSuccess)
     return ALOHA_ERR_CUDA;

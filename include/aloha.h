@@ -222,7 +222,8 @@ int aloha_composite_over_rgba8(const uint32_t* rank_fbs, const int* order, int n
  * reference counterpart.  It allocates nothing: the composite order is staged
  * in a 16 KB device array compiled into the library (held by every GPU that
  * loads it until exit), whose address is looked up on the first call made on
- * each device, so that first call should come before any stream capture.
+ * each device.  It cannot be recorded into a CUDA graph: on a capturing
+ * stream it returns ALOHA_ERR_UNSUPPORTED and leaves the capture untouched.
  * rank_images and fb must be device memory of the current device, order host
  * memory; at most 4096 ranks (else ALOHA_ERR_OUT_OF_RANGE).  The call reads
  * `order` once into a private host snapshot, checks it and copies the

@@ -83,3 +83,29 @@ def test_noalloc_composite_rejects_what_it_cannot_serve():
                                           None) == abi.ERR_OUT_OF_RANGE
     assert L.aloha_composite_over_noalloc(None, order.ctypes.data, 2, 8, 8, 0, fb.data_ptr(),
                                           None) == abi.ERR_NULL_POINTER
+
+
+def test_noalloc_composite_refuses_stream_capture():
+    """Its order copy is from pageable memory, which a capture cannot record:
+    on a capturing stream the call returns ALOHA_ERR_UNSUPPORTED without
+    touching the stream, and the caller's capture still ends and replays."""
+    torch = pytest.importorskip("torch")
+    from aloha_gb300 import abi
+    L = abi.lib()
+    n_ranks, H, W = 4, 32, 48
+    imgs = _images(torch, n_ranks, H, W, 9)
+    order = np.arange(n_ranks, dtype=np.int32)
+    fb = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+    x = torch.zeros(16, device="cuda")
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    with torch.cuda.graph(g, stream=side, capture_error_mode="relaxed"):
+        rc = L.aloha_composite_over_noalloc(imgs.data_ptr(), order.ctypes.data, n_ranks, W, H, 0, fb.data_ptr(),
+                                            torch.cuda.current_stream().cuda_stream)
+        x.add_(1.0)
+    assert rc == abi.ERR_UNSUPPORTED
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(x.sum()) == 16.0
+    assert int(fb.abs().sum()) == 0  # nothing was composited during the capture
