@@ -67,6 +67,9 @@ def parse():
     ap.add_argument("--batch-staging", choices=["tune", "0", "1"], default="tune",
                     help="with --only-batched: autotune, or fix the stencil staging at the 8x4 tile")
     ap.add_argument("--profile", action="store_true", help="short run for ncu (no baselines, no clocks)")
+    ap.add_argument("--reference-kind", choices=["auto", "reference", "port"], default="auto",
+                    help="--impl reference: time the reference's own CPU-compiled raygen (oracle/_ref, where its "
+                         "sources or build are present), the CPU restatement, or the first available")
     return ap.parse_args()
 
 
@@ -225,9 +228,28 @@ def workload_config(args, n_cams, world):
             "seeds": {"volume": 2001, "cameras": 2002}}
 
 
+def reference_kind(requested: str) -> str:
+    """"reference": the reference's own deviceCode.cpp raygen and Partitioner,
+    compiled on the CPU from its sources (oracle/_ref), usable wherever those
+    sources are present or that build exists for this machine; "port": the
+    CPU restatement (oracle/), which runs everywhere."""
+    if requested == "port":
+        return "port"
+    try:
+        from oracle import reference as R
+        ok = R.loadable()
+    except Exception:
+        ok = False
+    if requested == "reference" and not ok:
+        raise SystemExit("--reference-kind reference: the reference build is not available here")
+    return "reference" if ok else "port"
+
+
 def reference_arm(args):
-    """--impl reference: the CPU restatement of the reference path on all host
-    cores (the reference's OptiX/MPI/IceT build is unavailable), rank 0 only."""
+    """--impl reference: the reference path on all host cores, rank 0 only.
+    The reference's OptiX/MPI/IceT build cannot run here; its own CPU-compiled
+    raygen and Partitioner (oracle/_ref) are timed where available, else the
+    CPU restatement."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -243,15 +265,22 @@ def reference_arm(args):
     threads = O.lib().ora_max_threads()
     params = O.make_params()
     rows_per_step = 16
+    kind = reference_kind(args.reference_kind)
+    if kind == "reference":
+        from oracle import reference as R
+        band = R.BandRenderer(descs, vox, tf, W, W, 8, dt=params.dt, jitter_mode=params.jitter_mode,
+                              threads=threads)
 
     # step k: band k % 8 of view k // 8, 16 rows starting at a multiple of
     # H/8 (the bands the GPU arm's cpu_baseline samples)
     def step(k):
         cam = O.make_camera(*cams[(k // 8) % len(cams)])
-        sch = O.schedule(descs, 8, list(cam.org))
         y0 = (k % 8) * (W // 8)
-        r = O.render(descs, vox, tf, cam, W, W, params, sched=sch, rows=(y0, min(W, y0 + rows_per_step)),
-                     threads=threads, want=())
+        rows = (y0, min(W, y0 + rows_per_step))
+        if kind == "reference":
+            return band.render(cam, rows)[1]
+        sch = O.schedule(descs, 8, list(cam.org))
+        r = O.render(descs, vox, tf, cam, W, W, params, sched=sch, rows=rows, threads=threads, want=())
         return r["samples"]
 
     for k in range(args.warmup):
@@ -267,7 +296,7 @@ def reference_arm(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
             "config": workload_config(args, len(cams), args.gpus),
             "step": "one 16-row band of one view (8 bands per view, every H/8 rows)",
-            "cpu_baseline": {"value": g, "unit": "Gsamples/s", "cores": threads, "kind": "port",
+            "cpu_baseline": {"value": g, "unit": "Gsamples/s", "cores": threads, "kind": kind,
                              "sample": f"{args.steps} steps x {rows_per_step} rows x {W} pixels"},
             "e2e": {"value": g, "unit": "Gsamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

@@ -189,17 +189,21 @@ void owl::aloha_ref_trace(OptixTraversableHandle group, const Ray& ray, void* pr
 // ------------------------------------------------------------- C API
 extern "C" {
 
-// One rank's frame through the reference raygen.  bricks: the rank's bricks
-// as .vol headers (80 bytes each, in the rank's load order); voxels: their
-// voxel ranges, x fastest; test_order: local brick indices front to back;
-// tf: n_tf RGBA entries; cam: org, dir_00, dir_du, dir_dv.  accum: W*H float4
-// (read when accum_id > 0, always written, as renderFrame does).  Outputs: fb
-// (RGBA8), depth, per-pixel sample counts.
-int ref_render_rank(const aloha_oracle::BrickDesc* bricks, const float* const* voxels, int n_bricks,
-                    const int* test_order, int n_test, const float* tf, int n_tf, const float* cam, int width,
-                    int height, float dt, float max_depth, int spp, int accum_id, int jitter_mode,
-                    float jitter_value, float* accum, uint32_t* fb, float* depth, uint32_t* samples, int threads) {
+// Rows [y0, y1) of one rank's frame through the reference raygen (pixel ids,
+// and with them the jitter draws, are those of the whole width x height
+// frame; only those rows of the outputs are written).  bricks: the rank's
+// bricks as .vol headers (80 bytes each, in the rank's load order); voxels:
+// their voxel ranges, x fastest; test_order: local brick indices front to
+// back; tf: n_tf RGBA entries; cam: org, dir_00, dir_du, dir_dv.  accum: W*H
+// float4 (read when accum_id > 0, always written, as renderFrame does).
+// Outputs: fb (RGBA8), depth, per-pixel sample counts.
+int ref_render_rank_rows(const aloha_oracle::BrickDesc* bricks, const float* const* voxels, int n_bricks,
+                         const int* test_order, int n_test, const float* tf, int n_tf, const float* cam, int width,
+                         int height, float dt, float max_depth, int spp, int accum_id, int jitter_mode,
+                         float jitter_value, float* accum, uint32_t* fb, float* depth, uint32_t* samples, int y0,
+                         int y1, int threads) {
   if (n_bricks < 0 || width < 1 || height < 1 || n_tf < 1 || spp < 1) return -1;
+  if (y0 < 0 || y1 > height || y0 >= y1) return -1;
   std::vector<maui::VolBrick> vb(n_bricks);
   g_volumes.resize(n_bricks);
   for (int b = 0; b < n_bricks; ++b) {
@@ -249,7 +253,7 @@ int ref_render_rank(const aloha_oracle::BrickDesc* bricks, const float* const* v
   lp.render.spp = spp;
 
 #pragma omp parallel for schedule(dynamic, 1) num_threads(threads > 0 ? threads : omp_get_max_threads())
-  for (int y = 0; y < height; ++y) {
+  for (int y = y0; y < y1; ++y) {
     for (int x = 0; x < width; ++x) {
       t_state.x = x;
       t_state.y = y;
@@ -259,6 +263,16 @@ int ref_render_rank(const aloha_oracle::BrickDesc* bricks, const float* const* v
     }
   }
   return 0;
+}
+
+// The whole frame.
+int ref_render_rank(const aloha_oracle::BrickDesc* bricks, const float* const* voxels, int n_bricks,
+                    const int* test_order, int n_test, const float* tf, int n_tf, const float* cam, int width,
+                    int height, float dt, float max_depth, int spp, int accum_id, int jitter_mode,
+                    float jitter_value, float* accum, uint32_t* fb, float* depth, uint32_t* samples, int threads) {
+  return ref_render_rank_rows(bricks, voxels, n_bricks, test_order, n_test, tf, n_tf, cam, width, height, dt,
+                              max_depth, spp, accum_id, jitter_mode, jitter_value, accum, fb, depth, samples, 0,
+                              height, threads);
 }
 
 // partitionKD over n boxes (space ranges, lo xyz hi xyz) for n_ranks ranks,

@@ -1,9 +1,10 @@
 """bench.py's reference arm on the CPU: one JSON line with the contract's keys.
 
-`bench.py --impl reference` times the CPU restatement of the reference path
-(the oracle) on the host cores, on the same metric, unit and config as the
-GPU arm; under several ranks only rank 0 prints.  Run here at a small volume
-and image so that it takes a few seconds.
+`bench.py --impl reference` times the reference path on the host cores: the
+reference's own raygen compiled on the CPU (oracle/_ref) where its sources or
+build are present, else the CPU restatement (the oracle), on the same metric,
+unit and config as the GPU arm; under several ranks only rank 0 prints.  Run
+here at a small volume and image so that it takes a few seconds.
 """
 import json
 import os
@@ -16,19 +17,22 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ARGS = ["--impl", "reference", "--n", "64", "--size", "64", "--cameras", "4", "--steps", "3", "--warmup", "3"]
 
 
-def _run(env_extra=None):
+def _run(env_extra=None, extra=()):
     env = dict(os.environ)
     env.update(env_extra or {})
-    return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py")] + ARGS, capture_output=True, text=True,
-                          timeout=600, env=env, cwd=ROOT)
+    return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py")] + ARGS + list(extra), capture_output=True,
+                          text=True, timeout=600, env=env, cwd=ROOT)
 
 
-def test_reference_arm_prints_the_contract_line():
-    out = _run()
+def _line(out):
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [ln for ln in out.stdout.splitlines() if ln.strip()]
     assert len(lines) == 1
-    d = json.loads(lines[0])
+    return json.loads(lines[0])
+
+
+def test_reference_arm_prints_the_contract_line():
+    d = _line(_run())
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
                 "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
         assert key in d, key
@@ -43,10 +47,26 @@ def test_reference_arm_prints_the_contract_line():
     args = type("A", (), {"n": 64, "size": 64})()
     assert d["config"] == bench.workload_config(args, 4, 1)
     cb = d["cpu_baseline"]
-    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    from oracle import reference as R
+    assert cb["kind"] == ("reference" if R.loadable() else "port")
+    assert cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_kinds_time_the_same_samples():
+    """The reference's own build and the restatement march the same bands:
+    their sample counts (value x time) agree to the pinned tolerance."""
+    sys.path.insert(0, ROOT)
+    from oracle import reference as R
+    if not R.available():
+        pytest.skip("the reference sources are not present")
+    port = _line(_run(extra=["--reference-kind", "port"]))
+    ref = _line(_run(extra=["--reference-kind", "reference"]))
+    assert port["cpu_baseline"]["kind"] == "port" and ref["cpu_baseline"]["kind"] == "reference"
+    samples = [d["value"] * 1e9 * d["ms_per_step"] * 1e-3 * d["steps"] for d in (port, ref)]
+    assert abs(samples[0] - samples[1]) <= 1e-3 * samples[0]
 
 
 def test_reference_arm_other_ranks_print_nothing():
