@@ -607,11 +607,23 @@ int check_params(aloha_ctx* c, const aloha_render_params* p) {
   return ALOHA_OK;
 }
 
-int set_partition(aloha_ctx* c, int n_ranks) {
+// partitionKD over n_ranks ranks.  It splits a group at the midplane of its
+// bounds' longest axis, so bricks that are separated only along a shorter
+// axis cannot be split (the reference repeats that split forever): an
+// error, unless `identity_fallback` (one rank per brick, as set_bricks
+// resets it), where brick b then goes to rank b without a KD tree, like an
+// explicit assignment.  With one brick per rank either numbering gives the
+// same frames.
+int set_partition(aloha_ctx* c, int n_ranks, bool identity_fallback = false) {
   std::vector<int> br;
   std::vector<KdNode> tree;
-  if (!partition_kd(c->boxes, n_ranks, br, tree))
-    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "partitionKD made no progress for %d ranks", n_ranks);
+  if (!partition_kd(c->boxes, n_ranks, br, tree)) {
+    if (!identity_fallback || n_ranks != (int)c->boxes.size())
+      return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "partitionKD made no progress for %d ranks", n_ranks);
+    br.resize(n_ranks);
+    for (int b = 0; b < n_ranks; ++b) br[b] = b;
+    tree.clear();
+  }
   c->n_ranks = n_ranks;
   c->brick_rank = br;
   c->tree = tree;
@@ -871,7 +883,7 @@ int aloha_set_bricks(aloha_ctx* c, const aloha_brick_desc* descs, const float* c
   }
   c->staging_in.release();
   c->sched_stride = 0;
-  return set_partition(c, n);
+  return set_partition(c, n, true);
 }
 
 int aloha_update_brick(aloha_ctx* c, int brick, const float* voxels) {

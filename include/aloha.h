@@ -105,7 +105,8 @@ int aloha_set_render_params(aloha_ctx* ctx, const aloha_render_params* params);
 /* Upload `n` bricks (replaces the brick upload of waikikiRenderer.cpp:637-777).
  * voxels[i] holds brick i's voxel range, x fastest, float32 (host or device).
  * The library keeps its own device copy.  Resets the rank partition to one
- * rank per brick. */
+ * rank per brick: partitionKD's numbering, or brick i -> rank i for brick sets
+ * partitionKD cannot split (see aloha_set_ranks); frames are the same. */
 int aloha_set_bricks(aloha_ctx* ctx, const aloha_brick_desc* descs, const float* const* voxels, int n);
 
 /* Replace one brick's voxels (same voxel range), e.g. after a density update. */
@@ -123,7 +124,11 @@ int aloha_set_transfer_function(aloha_ctx* ctx, const float* rgba, int n);
 
 /* Virtual ranks: partitionKD of the bricks over n_ranks ranks
  * (waikikiRenderer.cpp:150-270, called at 630-631), or an explicit
- * assignment brick -> rank. */
+ * assignment brick -> rank.  partitionKD splits a group at the midplane of
+ * its bounds' longest axis; where the bricks of a group are separated only
+ * along a shorter axis that split makes no progress (the reference repeats it
+ * forever) and aloha_set_ranks returns ALOHA_ERR_INVALID_ARGUMENT: use
+ * aloha_set_rank_assignment for such brick sets. */
 int aloha_set_ranks(aloha_ctx* ctx, int n_ranks);
 int aloha_set_rank_assignment(aloha_ctx* ctx, const int* brick_rank, int n_bricks, int n_ranks);
 

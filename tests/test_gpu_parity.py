@@ -601,3 +601,35 @@ def test_full_size_rows_bit_exact(gpu_ctx_factory, oracle):
                                 rows=(y0, y0 + 2))
             assert_same_fb(fb[y0:y0 + 2], ref["fb"][y0:y0 + 2])
         assert samples > 1e7
+
+
+def test_bricks_that_partitionkd_cannot_split(gpu_ctx_factory, oracle):
+    """Two bricks separated only along y, in a volume whose longest axis is x:
+    partitionKD's midplane split on x leaves both on one side, forever in the
+    reference.  Uploading them still works (one rank per brick, brick i on
+    rank i), aloha_set_ranks(2) refuses, and the frame equals the oracle's
+    with that explicit assignment."""
+    dims = (64, 24, 20)
+    vol = S.blob_field(dims, 6, (2.0, 6.0), seed=5)
+    descs = S.grid_split(dims, ([], [12], []))
+    vox = S.extract_bricks(vol, descs)
+    tf = S.ramp_tf()
+    with pytest.raises(ValueError):
+        oracle.partition_kd(descs, 2)
+    ctx = gpu_ctx_factory()
+    ctx.set_bricks(descs, vox)
+    ctx.set_transfer_function(tf)
+    W, H = 64, 48
+    cam = S.look_at_camera([32.0, 80.0, -60.0], [32.0, 12.0, 10.0], [0, 1, 0], 40.0, W, H)
+    identity = np.arange(2, dtype=np.int32)
+    fb, samples = gpu_frame(ctx, cam, W, H)
+    ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H, oracle.make_params(), n_ranks=2,
+                        brick_rank=identity)
+    assert_same_fb(fb, ref["fb"])
+    assert samples == ref["samples"]
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.set_ranks(2)
+    assert e.value.code == abi.ERR_INVALID_ARGUMENT
+    ctx.set_ranks(1)  # one rank always partitions
+    fb1, _ = gpu_frame(ctx, cam, W, H)
+    assert_same_fb(fb1, oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=1)["fb"])
