@@ -16,6 +16,11 @@ make one at a time:
   staging and lane groups.
 
 Frames and sample counts must be bit-identical to the oracle, as everywhere.
+Two more sweeps draw the batched launch (1 to 10 views of random sizes, every
+chunk shape, CTA count and staging, plain or graph launch; each view's frame
+bit-identical to the oracle's) and the differentiable form (random
+single-rank scenes and checkpoint intervals; the training forward's float
+image bit-identical, both gradients within 1e-3 of the FP64 adjoint).
 """
 import numpy as np
 import pytest
@@ -150,3 +155,117 @@ def test_random_configuration_bit_exact(gpu_ctx_factory, oracle, seed):
         raise AssertionError(f"{where}: {len(diff)} pixels differ; first at ({x},{y}): "
                              f"{fb[y, x]:08x} vs {ref['fb'][y, x]:08x}")
     assert samples == ref["samples"], where
+
+
+def _partitioned(oracle, ctx, descs, n_ranks, rng):
+    """Ranks by partitionKD where it can split the bricks, else a random
+    assignment that uses every rank; returns the oracle's brick_rank."""
+    try:
+        oracle.partition_kd(descs, n_ranks)
+        ctx.set_ranks(n_ranks)
+        return None
+    except ValueError:
+        nb = len(descs)
+        br = np.concatenate([np.arange(n_ranks), rng.integers(0, n_ranks, nb - n_ranks)]).astype(np.int32)
+        rng.shuffle(br)
+        ctx.set_rank_assignment(br, n_ranks)
+        return br
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_random_batch_bit_exact(gpu_ctx_factory, oracle, seed):
+    """One persistent launch (plain or graph-captured) over 1 to 10 views of
+    random sizes and cameras, at a random chunk shape, CTA count and staging:
+    every view's frame equals the oracle's."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(5000 + seed)
+    dims = tuple(int(x) for x in rng.integers(9, 65, size=3))
+    vol = _volume(rng, dims)
+    descs = _bricks(rng, dims)
+    vox = S.extract_bricks(vol, descs)
+    tf = _tf(rng)
+    ctx = gpu_ctx_factory()
+    ctx.set_bricks(descs, vox)
+    ctx.set_transfer_function(tf)
+    n_ranks = int(rng.integers(1, len(descs) + 1))
+    brick_rank = _partitioned(oracle, ctx, descs, n_ranks, rng)
+    params = dict(dt=float(rng.choice([0.5, 1.0, 0.3, 0.375])), et_alpha=float(rng.choice([0.99, 0.6, 2.0])),
+                  jitter_mode=int(rng.choice([abi.JITTER_NONE, abi.JITTER_CONST, abi.JITTER_HASH])),
+                  jitter_value=float(rng.uniform()), spp=int(rng.choice([1, 2])),
+                  composite_mode=int(rng.choice([abi.COMPOSITE_FP32, abi.COMPOSITE_UBYTE])),
+                  crosshair=int(rng.random() < 0.2))
+    ctx.set_params(**params)
+    n_views = int(rng.integers(1, 11))
+    views = [int(v) for v in rng.permutation(16)[:n_views]]
+    sizes, cams = [], []
+    for v in views:
+        W, H = (int(x) for x in rng.choice([1, 9, 40, 64, 96], p=[.05, .15, .3, .25, .25], size=2))
+        cam = _camera(rng, dims, W, H)
+        ctx.set_camera(v, *cam)
+        ctx.resize(v, W, H)
+        sizes.append((W, H))
+        cams.append(cam)
+    fbs = [torch.full((H, W), -1, dtype=torch.int32, device="cuda") for (W, H) in sizes]
+    b = ctx.batch(views, fbs)
+    tile = [(8, 4), (8, 8), (16, 8), (32, 4)][int(rng.integers(0, 4))]
+    b.set_config(*tile, int(rng.choice([0, 3, 5, 7])))
+    b.set_staging(int(rng.choice([abi.STAGING_NONE, abi.STAGING_NEXT_SAMPLE])))
+    if rng.random() < 0.5:
+        b.launch()
+    else:
+        b.launch_graph()
+        b.launch_graph()
+    torch.cuda.synchronize()
+    for f, (W, H), cam in zip(fbs, sizes, cams):
+        ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H, oracle.make_params(**params),
+                            n_ranks=n_ranks, brick_rank=brick_rank, want=("fb",))
+        got = f.cpu().numpy().view(np.uint32)
+        assert np.array_equal(got, ref["fb"]), \
+            f"seed {seed}: view {W}x{H}, {np.count_nonzero(got != ref['fb'])} pixels differ, tile {tile}"
+    b.close()
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_differentiable_case(gpu_ctx_factory, oracle, seed):
+    """The differentiable form on random single-rank scenes: the training
+    forward's float image is bit-identical to the oracle's, and the gradients
+    of a random dL/dRGBA are within 1e-3 (relative 2-norm) of the FP64
+    adjoint, for a random checkpoint interval."""
+    rng = np.random.default_rng(9000 + seed)
+    dims = tuple(int(x) for x in rng.integers(9, 49, size=3))
+    vol = _volume(rng, dims)
+    descs = _bricks(rng, dims)
+    vox = S.extract_bricks(vol, descs)
+    tf = _tf(rng)
+    params = dict(dt=float(rng.choice([0.5, 1.0, 0.3, 0.375])), et_alpha=float(rng.choice([0.99, 0.8, 2.0])),
+                  jitter_mode=int(rng.choice([abi.JITTER_NONE, abi.JITTER_CONST, abi.JITTER_HASH])),
+                  jitter_value=float(rng.uniform()))
+    ctx = gpu_ctx_factory()
+    ctx.set_bricks(descs, vox)
+    ctx.set_transfer_function(tf)
+    ctx.set_ranks(1)
+    ctx.set_params(**params)
+    W, H = (int(x) for x in rng.choice([7, 33, 64], size=2))
+    cam = _camera(rng, dims, W, H)
+    ctx.set_camera(0, *cam)
+    ctx.resize(0, W, H)
+    k = int(rng.choice([1, 5, 16, 32, 64]))
+    img = np.zeros((H, W, 4), np.float32)
+    ctx.forward(0, img, k)
+    op = oracle.make_params(**params)
+    ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H, op, n_ranks=1, want=("final",))
+    np.testing.assert_array_equal(img, ref["final"])
+    dl = rng.uniform(-1, 1, (H, W, 4)).astype(np.float32)
+    nx, ny, nz = dims
+    dtf = np.zeros((tf.shape[0], 4), np.float32)
+    dden = np.zeros((nz, ny, nx), np.float32)
+    ctx.backward(0, dl, dtf, dden, (0, 0, 0), (nx, ny, nz))
+    r = oracle.adjoint(descs, vox, tf, oracle.make_camera(*cam), W, H, dl, (0, 0, 0), (nx, ny, nz), op)
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+    where = f"seed {seed}: dims {dims}, {len(descs)} bricks, {W}x{H}, K {k}, {params}, n_tf {tf.shape[0]}"
+    if np.linalg.norm(r["dtf"]) > 0:
+        assert rel(dtf, r["dtf"]) < 1e-3, where
+    if np.linalg.norm(r["ddensity"]) > 0:
+        assert rel(dden, r["ddensity"]) < 1e-3, where
