@@ -20,7 +20,8 @@ Two more sweeps draw the batched launch (1 to 10 views of random sizes, every
 chunk shape, CTA count and staging, plain or graph launch; each view's frame
 bit-identical to the oracle's) and the differentiable form (random
 single-rank scenes and checkpoint intervals; the training forward's float
-image bit-identical, both gradients within 1e-3 of the FP64 adjoint).
+image bit-identical, both gradients within 1e-3 of the FP64 adjoint).  A
+last one drives one context through random call sequences.
 """
 import numpy as np
 import pytest
@@ -269,3 +270,105 @@ def test_random_differentiable_case(gpu_ctx_factory, oracle, seed):
         assert rel(dtf, r["dtf"]) < 1e-3, where
     if np.linalg.norm(r["ddensity"]) > 0:
         assert rel(dden, r["ddensity"]) < 1e-3, where
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_call_sequences(gpu_ctx_factory, oracle, seed):
+    """One context driven through a seeded random sequence of 14 calls:
+    cameras, resizes, transfer functions (of other sizes too), brick updates
+    and drops, rank changes, render parameters and the work division.  After
+    each call the frame of a random view that has a camera and a size must
+    equal the oracle's for the state the calls built (a dropped brick must
+    make renders fail until its data is back).  This checks what the context
+    caches (view schedules, split planes, chunk orders, macrocell tables)
+    against every kind of change."""
+    rng = np.random.default_rng(7000 + seed)
+    dims = tuple(int(x) for x in rng.integers(12, 57, size=3))
+    vol = _volume(rng, dims)
+    descs = _bricks(rng, dims)
+    nb = len(descs)
+    vox = [np.ascontiguousarray(v) for v in S.extract_bricks(vol, descs)]
+    tf = _tf(rng)
+    ctx = gpu_ctx_factory()
+    ctx.set_bricks(descs, vox)
+    ctx.set_transfer_function(tf)
+    st = dict(n_ranks=nb, brick_rank=None, params={}, views={}, dropped=set())
+    try:
+        oracle.partition_kd(descs, nb)
+    except ValueError:
+        st["brick_rank"] = np.arange(nb, dtype=np.int32)  # the upload's fallback numbering
+
+    def set_camera(v):
+        W, H = (int(x) for x in rng.choice([9, 33, 64, 80], size=2))
+        cam = _camera(rng, dims, W, H)
+        ctx.set_camera(v, *cam)
+        old = st["views"].get(v, {})
+        st["views"][v] = dict(old, cam=cam)
+        if "size" not in old:
+            ctx.resize(v, W, H)
+            st["views"][v]["size"] = (W, H)
+
+    ops = ["camera", "resize", "tf", "update", "drop", "ranks", "assign", "params", "work"]
+    for step in range(14):
+        op = "camera" if not st["views"] else str(rng.choice(ops))
+        if op == "camera":
+            set_camera(int(rng.integers(0, 4)))
+        elif op == "resize":
+            v = int(rng.choice(list(st["views"])))
+            W, H = (int(x) for x in rng.choice([1, 9, 33, 64, 80], size=2))
+            ctx.resize(v, W, H)
+            st["views"][v]["size"] = (W, H)
+        elif op == "tf":
+            tf = _tf(rng)
+            ctx.set_transfer_function(tf)
+        elif op == "update":
+            b = int(rng.integers(0, nb))
+            vox[b] = np.ascontiguousarray((vox[b] * np.float32(rng.uniform(0.3, 1.5))).astype(np.float32))
+            ctx.update_brick(b, vox[b])
+            st["dropped"].discard(b)
+        elif op == "drop":
+            b = int(rng.integers(0, nb))
+            ctx.drop_brick(b)
+            st["dropped"].add(b)
+        elif op in ("ranks", "assign"):
+            n = int(rng.integers(1, nb + 1))
+            if op == "ranks":
+                try:
+                    oracle.partition_kd(descs, n)
+                except ValueError:
+                    with pytest.raises(abi.AlohaError):
+                        ctx.set_ranks(n)
+                    continue
+                ctx.set_ranks(n)
+                st["n_ranks"], st["brick_rank"] = n, None
+            else:
+                br = np.concatenate([np.arange(n), rng.integers(0, n, nb - n)]).astype(np.int32)
+                rng.shuffle(br)
+                ctx.set_rank_assignment(br, n)
+                st["n_ranks"], st["brick_rank"] = n, br
+        elif op == "params":
+            st["params"] = dict(dt=float(rng.choice([0.5, 1.0, 0.3])), et_alpha=float(rng.choice([0.99, 0.7, 2.0])),
+                                jitter_mode=int(rng.choice([abi.JITTER_NONE, abi.JITTER_CONST, abi.JITTER_HASH])),
+                                jitter_value=float(rng.uniform()),
+                                composite_mode=int(rng.choice([abi.COMPOSITE_FP32, abi.COMPOSITE_UBYTE])))
+            ctx.set_params(**st["params"])
+        elif op == "work":
+            split = int(rng.choice([abi.SPLIT_AUTO, abi.SPLIT_PIXELS, abi.SPLIT_RANKS]))
+            ctx.set_render_split(split)
+            ctx.set_chunk_order(int(rng.choice([abi.CHUNKS_AUTO, abi.CHUNKS_RING, abi.CHUNKS_PROBED])))
+            ctx.set_render_tile(*[(8, 4), (8, 8), (16, 8), (32, 4)][int(rng.integers(0, 4))])
+        v = int(rng.choice(list(st["views"])))
+        W, H = st["views"][v]["size"]
+        cam = st["views"][v]["cam"]
+        where = f"seed {seed} step {step} ({op}): view {v} {W}x{H}, {st['n_ranks']} ranks, {nb} bricks"
+        if st["dropped"]:
+            with pytest.raises(abi.AlohaError) as e:
+                ctx.render(v, width=W, height=H)
+            assert e.value.code == abi.ERR_MISSING_BRICK, where
+            continue
+        fb = ctx.render(v, width=W, height=H)
+        samples = ctx.stats().samples
+        ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H, oracle.make_params(**st["params"]),
+                            n_ranks=st["n_ranks"], brick_rank=st["brick_rank"], want=("fb",))
+        assert np.array_equal(fb, ref["fb"]), f"{where}: {np.count_nonzero(fb != ref['fb'])} pixels differ"
+        assert samples == ref["samples"], where
