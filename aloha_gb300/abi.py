@@ -38,7 +38,7 @@ EXPORTS = [
     "aloha_batch_autotune", "aloha_batch_destroy", "aloha_render_batch", "aloha_forward", "aloha_backward",
     "aloha_composite_over_noalloc", "aloha_set_render_tile", "aloha_set_render_split", "aloha_set_chunk_order",
     "aloha_set_render_staging", "aloha_batch_set_staging", "aloha_batch_get_staging", "aloha_set_lane_groups",
-    "aloha_backward_views",
+    "aloha_backward_views", "aloha_forward_views",
 ]
 
 
@@ -105,6 +105,7 @@ _SIGS = {
     "aloha_forward": ([P, I, P, I, P], I),
     "aloha_backward": ([P, I, P, P, P, P, P, P], I),
     "aloha_backward_views": ([P, I, P, P, P, P, P, P, P], I),
+    "aloha_forward_views": ([P, I, P, P, I, P], I),
     "aloha_composite_over_noalloc": ([P, P, I, I, I, I, P, P], I),
     "aloha_set_render_tile": ([P, I, I], I),
     "aloha_set_render_split": ([P, I], I),
@@ -304,6 +305,16 @@ class Context:
     def forward(self, view: int, rgba, checkpoint_every: int = 32, stream=None):
         """Differentiable render of `view` into float RGBA (H, W, 4); keeps checkpoints for backward()."""
         self._check(self._lib.aloha_forward(self.h, view, _addr(rgba), int(checkpoint_every), _stream(stream)))
+        return rgba
+
+    def forward_views(self, views, rgba, checkpoint_every: int = 32, stream=None):
+        """forward() of several views in one launch: rgba[i] (H, W, 4) receives views[i]'s image."""
+        n = len(views)
+        if len(rgba) != n:
+            raise ValueError("one image per view")
+        v = np.ascontiguousarray(views, dtype=np.int32)
+        ptrs = (P * n)(*[_addr(r) for r in rgba])
+        self._check(self._lib.aloha_forward_views(self.h, n, _addr(v), ptrs, int(checkpoint_every), _stream(stream)))
         return rgba
 
     def backward(self, view: int, dl_drgba, dl_dtf, dl_ddensity, grid_lo, grid_dims, stream=None):

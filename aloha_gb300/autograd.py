@@ -99,8 +99,14 @@ class _Render(torch.autograd.Function):
         renderer._upload(tf, density)
         stream = torch.cuda.current_stream()
         out = torch.empty((len(views), H, W, 4), dtype=torch.float32, device=density.device)
+        # all views in one launch (a view listed twice is rendered once and copied)
+        first = {}
         for i, v in enumerate(views):
-            renderer.ctx.forward(v, out[i], renderer.k, stream)
+            first.setdefault(v, i)
+        renderer.ctx.forward_views(list(first), [out[i] for i in first.values()], renderer.k, stream)
+        for i, v in enumerate(views):
+            if first[v] != i:
+                out[i].copy_(out[first[v]])
         ctx.renderer, ctx.views = renderer, list(views)
         ctx.tf_shape, ctx.density_shape = tf.shape, density.shape
         return out

@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <climits>
 
 #include "adjoint.h"
@@ -180,8 +181,8 @@ struct CheckpointHook {
 // colour is the render's bit for bit), checkpoints, final colour, and the
 // warp-aggregated append of (pixel, segment) items.  Returns the lane's
 // sample count.
-__device__ __forceinline__ uint32_t train_subtile(const TrainArgs& a, const DevView& v, const float4* tf_s, int x,
-                                                  int y, int lane) {
+__device__ __forceinline__ uint32_t train_subtile(const TrainArgs& a, const TrainView& tv, const DevView& v,
+                                                  const float4* tf_s, int x, int y, int lane) {
   const bool active = x < v.width && y < v.height;
   uint32_t n = 0, nseg = 0;
   uint32_t pixel = 0;
@@ -189,7 +190,7 @@ __device__ __forceinline__ uint32_t train_subtile(const TrainArgs& a, const DevV
     pixel = (uint32_t)x + (uint32_t)v.width * (uint32_t)y;
     const Ray ray = generate_ray(v, x, y);
     float4 color = make_float4(0.f, 0.f, 0.f, 0.f);
-    CheckpointHook hook{a.ckpt + (size_t)pixel * a.ckpt_cap, a.k, a.ckpt_cap, a.overflow};
+    CheckpointHook hook{tv.ckpt + (size_t)pixel * tv.ckpt_cap, a.k, tv.ckpt_cap, tv.overflow};
     const int* __restrict__ rb = rank_bricks(a, v);
     const int j1 = __ldg(a.sched + v.sched + 2);
     for (int j = 0; j < j1; ++j) {
@@ -202,9 +203,9 @@ __device__ __forceinline__ uint32_t train_subtile(const TrainArgs& a, const DevV
       hook.tmin = t1 + 1e-20f;
       if (!(color.w < a.et_alpha)) break;
     }
-    a.final_rgba[pixel] = color;
-    if (a.out_rgba) a.out_rgba[pixel] = color;
-    nseg = min((n + a.k - 1) / a.k, a.ckpt_cap);
+    tv.final_rgba[pixel] = color;
+    if (tv.out_rgba) tv.out_rgba[pixel] = color;
+    nseg = min((n + a.k - 1) / a.k, tv.ckpt_cap);
   }
   // warp-aggregated append of (pixel, segment) items, ordered by segment then
   // lane so that a backward warp replays neighbouring rays together
@@ -212,46 +213,66 @@ __device__ __forceinline__ uint32_t train_subtile(const TrainArgs& a, const DevV
   const unsigned total = __reduce_add_sync(full, nseg);
   const unsigned maxseg = __reduce_max_sync(full, nseg);
   unsigned base = 0;
-  if (lane == 0 && total) base = atomicAdd(a.work_count, total);
+  if (lane == 0 && total) base = atomicAdd(tv.work_count, total);
   base = __shfl_sync(full, base, 0);
   unsigned off = 0;
   for (unsigned m = 0; m < maxseg; ++m) {
     const unsigned mask = __ballot_sync(full, m < nseg);
     if (m < nseg) {
       const unsigned slot = base + off + __popc(mask & ((1u << lane) - 1u));
-      if (slot < a.work_cap) a.work[slot] = make_uint2(pixel, m);
+      if (slot < tv.work_cap) tv.work[slot] = make_uint2(pixel, m);
     }
     off += __popc(mask);
   }
   return n;
 }
 
-// Persistent training forward: warps pull 8 x 4 chunks (in cost order when
-// a.chunk_order is set, else centre-out, as the render does) from the counter
-// at work_count[1].
-__global__ void __launch_bounds__(128, kSingleRenderBlocks) forward_train_kernel(TrainArgs a, int view) {
+// Item `item` of a forward launch -> (view slot, chunk position): the run
+// holding it (binary search over the few runs), then position-major within
+// the run.
+__device__ __forceinline__ void forward_item(const TrainArgs& a, unsigned item, int& slot, int& pos) {
+  int lo = 0, hi = a.n_runs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&a.runs[mid].item0) <= item)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const int p0 = __ldg(&a.runs[lo].p0), active = __ldg(&a.runs[lo].active);
+  const unsigned off = item - __ldg(&a.runs[lo].item0);
+  pos = p0 + (int)(off / (unsigned)active);
+  slot = __ldg(a.run_views + off % (unsigned)active);
+}
+
+// Persistent training forward over the launch's views: warps pull items
+// (a view's 8 x 4 chunk, in its cost order when it has one, else
+// centre-out, as the render does) from the launch's counter.
+__global__ void __launch_bounds__(128, kSingleRenderBlocks) forward_train_kernel(TrainArgs a, unsigned items) {
   extern __shared__ float4 tf_s[];
   load_tf(tf_s, a.tf, a.n_tf);
   __syncthreads();
-  const DevView v = a.views[view];
   const int lane = threadIdx.x & 31;
-  const int cxn = (v.width + 7) / 8, cyn = (v.height + 3) / 4;
-  const int total = a.chunk_order ? a.n_chunks : ring_slots(v.width, v.height, 8, 4);
   uint32_t n = 0;
   for (;;) {
-    int chunk = 0;
-    if (lane == 0) chunk = (int)atomicAdd(a.work_count + 1, 1u);
-    chunk = __shfl_sync(0xffffffffu, chunk, 0);
-    if (chunk >= total) break;
+    unsigned item = 0;
+    if (lane == 0) item = atomicAdd(a.grab, 1u);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= items) break;
+    int slot, pos;
+    forward_item(a, item, slot, pos);
+    const TrainView& tv = a.tv[slot];
+    const DevView v = a.views[tv.view];
+    const int cxn = (v.width + 7) / 8, cyn = (v.height + 3) / 4;
     int ccx, ccy;
-    if (a.chunk_order) {
-      const int id = __ldg(a.chunk_order + chunk);
+    if (tv.chunk_order) {
+      const int id = __ldg(tv.chunk_order + pos);
       ccx = id % cxn;
       ccy = id / cxn;
-    } else if (!ring_chunk(chunk, cxn, cyn, ccx, ccy)) {
+    } else if (!ring_chunk(pos, cxn, cyn, ccx, ccy)) {
       continue;
     }
-    n += train_subtile(a, v, tf_s, ccx * 8 + (lane & 7), ccy * 4 + (lane >> 3), lane);
+    n += train_subtile(a, tv, v, tf_s, ccx * 8 + (lane & 7), ccy * 4 + (lane >> 3), lane);
   }
   count_samples(a.counter, n);
 }
@@ -423,14 +444,143 @@ __device__ __forceinline__ float4 suffix_composite(const TrainArgs& a, const Dev
 
 constexpr unsigned kBackwardGrab = 256;  // most items a backward warp takes per grab (8 rows of 32)
 
+// One backward item: the replay of segment (pixel, ck) of view v and its
+// adjoint, added to dtf_s (shared, WITH_TF) and the x-quad density gradient
+// (WITH_DENSITY).  Returns the samples replayed.
+template <bool WITH_TF, bool WITH_DENSITY>
+__device__ __forceinline__ uint32_t backward_item(const TrainArgs& a, const DevView& v, const int* __restrict__ rb,
+                                                  const float4* tf_s, float* dtf_s, float nf, uint32_t pixel,
+                                                  const Checkpoint& ck, const float4 F, const float4 g) {
+  const int x = (int)(pixel % (uint32_t)v.width), y = (int)(pixel / (uint32_t)v.width);
+  const Ray ray = generate_ray(v, x, y);
+  const float gfin = g.w * (1.0f - F.w);
+  float4 color = make_float4(ck.r, ck.g, ck.b, ck.a);
+  const Walk w0{(int)(ck.jd & 0xffffu), ck.tmin, ck.jd >> 16};
+  // transfer-function gradient of consecutive samples with the same lookup
+  // index is summed in registers and added to shared memory once per index
+  int pend_i = INT_MIN;
+  float pend[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  OpaqueEvent events[kMaxEvents];
+  int n_events = 0;
+  const uint32_t n = walk_samples<!WITH_TF>(
+      a, v, tf_s, ray, pixel, w0, ck.t, ck.nb, true, color, a.k,
+      [&](const DevBrick& b, float t, const Walk& wcur, uint32_t nb, float ux, float uy, float uz,
+          const StencilOut& s, float shade, const float4& c, const float4& col) {
+        // Backward-only arithmetic below is free to contract and to use
+        // approximate reciprocals (the gradient tolerance is relative); the
+        // replay that feeds it is the exact forward.
+        float4 nxt = col;  // state after this sample
+        composite_step(nxt, c, shade);
+        const float oma = 1.0f - col.w;
+        const float tn1 = 1.0f - nxt.w;
+        // dL/d(accumulated alpha after this sample), closed form
+        const float gA =
+            __fdividef(gfin - fmaf(g.x, F.x - nxt.x, fmaf(g.y, F.y - nxt.y, g.z * (F.z - nxt.z))),
+                       fmaxf(tn1, 1e-6f));
+        if (tn1 < kOpaqueStep * oma && oma > kVisible && n_events < kMaxEvents) {
+          OpaqueEvent& e = events[n_events++];
+          e.w = wcur;
+          e.t_next = t + a.dt;
+          e.nb_next = nb + 1;
+          e.after = nxt;
+          e.oma = oma;
+          e.gA = gA;
+          e.value = s.value;
+          e.ux = ux;
+          e.uy = uy;
+          e.uz = uz;
+          e.brick = __ldg(rb + wcur.j);
+        }
+        const float gc = fmaf(g.x, c.x, fmaf(g.y, c.y, g.z * c.z));
+        const float dA = oma * fmaf(shade, gc, gA);  // dL/d(alpha of this sample)
+        // transfer function lookup backward (the lookup of tf_lookup)
+        const float xb = s.value * nf - 0.5f;
+        const float fl = floorf(xb);
+        const float wt = xb - fl;
+        const int i0 = (int)fl;
+        const int ic = min(max(i0, -2), a.n_tf);
+        const float4 e0 = tf_s[ic + 2], e1 = tf_s[ic + 3];
+        if (WITH_TF && i0 != pend_i) {
+          flush_tf(dtf_s, a.n_tf, pend_i, pend);
+          pend_i = i0;
+        }
+        if (e0.w == 0.f && e1.w == 0.f) {
+          // Alpha is exactly 0 at this sample: only the two alpha entries of
+          // the lookup receive gradient; the colour entries, the shading and
+          // the density gradients all carry a factor alpha or d(alpha)/dv = 0.
+          if (WITH_TF) {
+            pend[3] = fmaf(1.f - wt, dA, pend[3]);
+            pend[7] = fmaf(wt, dA, pend[7]);
+          }
+          return;
+        }
+        const float kc = oma * c.w * shade;
+        const float dch[4] = {g.x * kc, g.y * kc, g.z * kc, dA};
+        if (WITH_TF) {
+  #pragma unroll
+          for (int ch = 0; ch < 4; ++ch) {
+            pend[ch] = fmaf(1.f - wt, dch[ch], pend[ch]);
+            pend[4 + ch] = fmaf(wt, dch[ch], pend[4 + ch]);
+          }
+        }
+        if (!WITH_DENSITY) return;
+        const float ds = oma * c.w * gc;
+        const float de[4] = {e1.x - e0.x, e1.y - e0.y, e1.z - e0.z, e1.w - e0.w};
+        float dv = 0.f;
+  #pragma unroll
+        for (int ch = 0; ch < 4; ++ch) dv = fmaf(dch[ch], de[ch], dv);
+        dv *= nf;
+        // shading backward: s = .1 + .9 |q|, q = (g.d)/|g + 1e-4|
+        const float ex = s.gx + 1e-4f, ey = s.gy + 1e-4f, ez = s.gz + 1e-4f;
+        const float len2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+        const float inv = rsqrtf(len2);
+        const float gd = fmaf(s.gx, ray.d[0], fmaf(s.gy, ray.d[1], s.gz * ray.d[2]));
+        const float kk = ds * 0.9f * (gd > 0.f ? 1.f : (gd < 0.f ? -1.f : 0.f));
+        const float c3 = gd * inv * inv * inv;
+        const float ki = kk * inv, kc3 = kk * c3;
+        stencil_backward(b, a, __ldg(rb + wcur.j), ux, uy, uz, dv, fmaf(ki, ray.d[0], -kc3 * ex),
+                         fmaf(ki, ray.d[1], -kc3 * ey), fmaf(ki, ray.d[2], -kc3 * ez));
+      });
+  if (WITH_TF) flush_tf(dtf_s, a.n_tf, pend_i, pend);
+  // near-opaque samples: correct the alpha adjoint by the true one
+  for (int k = 0; k < n_events; ++k) {
+    const OpaqueEvent& e = events[k];
+    const float4 R = suffix_composite(a, v, tf_s, ray, pixel, e);
+    const float gtrue = fmaf(g.w, R.w, -fmaf(g.x, R.x, fmaf(g.y, R.y, g.z * R.z)));
+    const float dd = e.oma * (gtrue - e.gA);  // change of dL/d(alpha of the sample)
+    if (dd == 0.f) continue;
+    const float xb = e.value * nf - 0.5f;
+    const float fl = floorf(xb);
+    const float wt = xb - fl;
+    const int i0 = (int)fl;
+    if (WITH_TF) {
+      if (i0 >= 0 && i0 < a.n_tf) atomicAdd(dtf_s + i0 * 4 + 3, (1.f - wt) * dd);
+      if (i0 + 1 >= 0 && i0 + 1 < a.n_tf) atomicAdd(dtf_s + (i0 + 1) * 4 + 3, wt * dd);
+    }
+    if (WITH_DENSITY) {
+      const int ic = min(max(i0, -2), a.n_tf);
+      const float dv = nf * dd * (tf_s[ic + 3].w - tf_s[ic + 2].w);
+      if (dv != 0.f) {
+        const DevBrick b = a.bricks[e.brick];
+        stencil_backward(b, a, e.brick, e.ux, e.uy, e.uz, dv, 0.f, 0.f, 0.f);
+      }
+    }
+  }
+  return n;
+}
+
 // WITH_TF: the transfer-function gradient; WITH_DENSITY: the density
 // gradient (at least one of them).  Without the transfer-function gradient
 // the replay skips empty macrocells like the forward: a sample there has
 // transfer-function alpha 0 at both lookup entries, so its density and
 // shading gradients vanish and only the alpha entries would receive any.
 // Without the density gradient the shading and stencil adjoints are skipped.
-template <bool WITH_TF, bool WITH_DENSITY>
-__global__ void __launch_bounds__(128, 5) backward_kernel(TrainArgs a, int view) {
+// MULTI: the launch's items belong to several views (item_base, tv), each
+// item looks its view up; else to the one view passed in the parameters
+// (a.one), whose pointers then stay in the constant bank, as the replay's
+// register budget wants.
+template <bool WITH_TF, bool WITH_DENSITY, bool MULTI>
+__global__ void __launch_bounds__(128, 5) backward_kernel(TrainArgs a) {
   extern __shared__ float4 smem[];
   float4* tf_s = smem;                                         // n_tf + 4 entries
   float* dtf_s = reinterpret_cast<float*>(smem + a.n_tf + 4);  // n_tf * 4 (WITH_TF)
@@ -438,11 +588,15 @@ __global__ void __launch_bounds__(128, 5) backward_kernel(TrainArgs a, int view)
   if (WITH_TF)
     for (int i = threadIdx.x; i < a.n_tf * 4; i += blockDim.x) dtf_s[i] = 0.f;
   __syncthreads();
-  const DevView v = a.views[view];
-  const int* __restrict__ rb = rank_bricks(a, v);
-  const unsigned count = min(*a.work_count, a.work_cap);
+  const unsigned count = MULTI ? __ldg(a.item_base + a.n_views) : a.one_items;
   const float nf = (float)a.n_tf;
   uint32_t nsamp = 0;
+  DevView v1{};
+  const int* rb1 = nullptr;
+  if constexpr (!MULTI) {
+    v1 = a.views[a.one.view];
+    rb1 = rank_bricks(a, v1);
+  }
   // Warps take kBackwardGrab consecutive items at a time.  The forward lays
   // out each of its 8x4 tiles as rows of 32 (segment m of every lane, then
   // m + 1, ...), so a warp replays consecutive segments of the same rays and
@@ -454,130 +608,31 @@ __global__ void __launch_bounds__(128, 5) backward_kernel(TrainArgs a, int view)
   const unsigned take = max(32u, min(kBackwardGrab, (count / (warps * 8u)) & ~31u));
   for (;;) {
     unsigned grab = 0;
-    if (lane == 0) grab = atomicAdd(a.work_count + 2, take);
+    if (lane == 0) grab = atomicAdd(a.grab, take);
     grab = __shfl_sync(0xffffffffu, grab, 0);
     if (grab >= count) break;
     const unsigned end = min(grab + take, count);
     for (unsigned item = grab + lane; item < end; item += 32u) {
-      const uint2 wk = a.work[item];
-      const uint32_t pixel = wk.x, m = wk.y;
-      const int x = (int)(pixel % (uint32_t)v.width), y = (int)(pixel / (uint32_t)v.width);
-      const Ray ray = generate_ray(v, x, y);
-      const Checkpoint ck = a.ckpt[(size_t)pixel * a.ckpt_cap + m];
-      const float4 F = a.final_rgba[pixel];
-      const float4 g = a.dl_drgba[pixel];
-      const float gfin = g.w * (1.0f - F.w);
-      float4 color = make_float4(ck.r, ck.g, ck.b, ck.a);
-      const Walk w0{(int)(ck.jd & 0xffffu), ck.tmin, ck.jd >> 16};
-      // transfer-function gradient of consecutive samples with the same lookup
-      // index is summed in registers and added to shared memory once per index
-      int pend_i = INT_MIN;
-      float pend[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      OpaqueEvent events[kMaxEvents];
-      int n_events = 0;
-      nsamp += walk_samples<!WITH_TF>(
-          a, v, tf_s, ray, pixel, w0, ck.t, ck.nb, true, color, a.k,
-          [&](const DevBrick& b, float t, const Walk& wcur, uint32_t nb, float ux, float uy, float uz,
-              const StencilOut& s, float shade, const float4& c, const float4& col) {
-            // Backward-only arithmetic below is free to contract and to use
-            // approximate reciprocals (the gradient tolerance is relative); the
-            // replay that feeds it is the exact forward.
-            float4 nxt = col;  // state after this sample
-            composite_step(nxt, c, shade);
-            const float oma = 1.0f - col.w;
-            const float tn1 = 1.0f - nxt.w;
-            // dL/d(accumulated alpha after this sample), closed form
-            const float gA =
-                __fdividef(gfin - fmaf(g.x, F.x - nxt.x, fmaf(g.y, F.y - nxt.y, g.z * (F.z - nxt.z))),
-                           fmaxf(tn1, 1e-6f));
-            if (tn1 < kOpaqueStep * oma && oma > kVisible && n_events < kMaxEvents) {
-              OpaqueEvent& e = events[n_events++];
-              e.w = wcur;
-              e.t_next = t + a.dt;
-              e.nb_next = nb + 1;
-              e.after = nxt;
-              e.oma = oma;
-              e.gA = gA;
-              e.value = s.value;
-              e.ux = ux;
-              e.uy = uy;
-              e.uz = uz;
-              e.brick = __ldg(rb + wcur.j);
-            }
-            const float gc = fmaf(g.x, c.x, fmaf(g.y, c.y, g.z * c.z));
-            const float dA = oma * fmaf(shade, gc, gA);  // dL/d(alpha of this sample)
-            // transfer function lookup backward (the lookup of tf_lookup)
-            const float xb = s.value * nf - 0.5f;
-            const float fl = floorf(xb);
-            const float wt = xb - fl;
-            const int i0 = (int)fl;
-            const int ic = min(max(i0, -2), a.n_tf);
-            const float4 e0 = tf_s[ic + 2], e1 = tf_s[ic + 3];
-            if (WITH_TF && i0 != pend_i) {
-              flush_tf(dtf_s, a.n_tf, pend_i, pend);
-              pend_i = i0;
-            }
-            if (e0.w == 0.f && e1.w == 0.f) {
-              // Alpha is exactly 0 at this sample: only the two alpha entries of
-              // the lookup receive gradient; the colour entries, the shading and
-              // the density gradients all carry a factor alpha or d(alpha)/dv = 0.
-              if (WITH_TF) {
-                pend[3] = fmaf(1.f - wt, dA, pend[3]);
-                pend[7] = fmaf(wt, dA, pend[7]);
-              }
-              return;
-            }
-            const float kc = oma * c.w * shade;
-            const float dch[4] = {g.x * kc, g.y * kc, g.z * kc, dA};
-            if (WITH_TF) {
-  #pragma unroll
-              for (int ch = 0; ch < 4; ++ch) {
-                pend[ch] = fmaf(1.f - wt, dch[ch], pend[ch]);
-                pend[4 + ch] = fmaf(wt, dch[ch], pend[4 + ch]);
-              }
-            }
-            if (!WITH_DENSITY) return;
-            const float ds = oma * c.w * gc;
-            const float de[4] = {e1.x - e0.x, e1.y - e0.y, e1.z - e0.z, e1.w - e0.w};
-            float dv = 0.f;
-  #pragma unroll
-            for (int ch = 0; ch < 4; ++ch) dv = fmaf(dch[ch], de[ch], dv);
-            dv *= nf;
-            // shading backward: s = .1 + .9 |q|, q = (g.d)/|g + 1e-4|
-            const float ex = s.gx + 1e-4f, ey = s.gy + 1e-4f, ez = s.gz + 1e-4f;
-            const float len2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-            const float inv = rsqrtf(len2);
-            const float gd = fmaf(s.gx, ray.d[0], fmaf(s.gy, ray.d[1], s.gz * ray.d[2]));
-            const float kk = ds * 0.9f * (gd > 0.f ? 1.f : (gd < 0.f ? -1.f : 0.f));
-            const float c3 = gd * inv * inv * inv;
-            const float ki = kk * inv, kc3 = kk * c3;
-            stencil_backward(b, a, __ldg(rb + wcur.j), ux, uy, uz, dv, fmaf(ki, ray.d[0], -kc3 * ex),
-                             fmaf(ki, ray.d[1], -kc3 * ey), fmaf(ki, ray.d[2], -kc3 * ez));
-          });
-      if (WITH_TF) flush_tf(dtf_s, a.n_tf, pend_i, pend);
-      // near-opaque samples: correct the alpha adjoint by the true one
-      for (int k = 0; k < n_events; ++k) {
-        const OpaqueEvent& e = events[k];
-        const float4 R = suffix_composite(a, v, tf_s, ray, pixel, e);
-        const float gtrue = fmaf(g.w, R.w, -fmaf(g.x, R.x, fmaf(g.y, R.y, g.z * R.z)));
-        const float dd = e.oma * (gtrue - e.gA);  // change of dL/d(alpha of the sample)
-        if (dd == 0.f) continue;
-        const float xb = e.value * nf - 0.5f;
-        const float fl = floorf(xb);
-        const float wt = xb - fl;
-        const int i0 = (int)fl;
-        if (WITH_TF) {
-          if (i0 >= 0 && i0 < a.n_tf) atomicAdd(dtf_s + i0 * 4 + 3, (1.f - wt) * dd);
-          if (i0 + 1 >= 0 && i0 + 1 < a.n_tf) atomicAdd(dtf_s + (i0 + 1) * 4 + 3, wt * dd);
+      if constexpr (MULTI) {
+        int slot = 0;  // item_base[slot] <= item < item_base[slot + 1]
+        for (int hi = a.n_views - 1; slot < hi;) {
+          const int mid = (slot + hi + 1) >> 1;
+          if (__ldg(a.item_base + mid) <= item)
+            slot = mid;
+          else
+            hi = mid - 1;
         }
-        if (WITH_DENSITY) {
-          const int ic = min(max(i0, -2), a.n_tf);
-          const float dv = nf * dd * (tf_s[ic + 3].w - tf_s[ic + 2].w);
-          if (dv != 0.f) {
-            const DevBrick b = a.bricks[e.brick];
-            stencil_backward(b, a, e.brick, e.ux, e.uy, e.uz, dv, 0.f, 0.f, 0.f);
-          }
-        }
+        const TrainView& tv = a.tv[slot];
+        const DevView v = a.views[tv.view];
+        const uint2 wk = tv.work[item - __ldg(a.item_base + slot)];
+        const Checkpoint ck = tv.ckpt[(size_t)wk.x * tv.ckpt_cap + wk.y];
+        nsamp += backward_item<WITH_TF, WITH_DENSITY>(a, v, rank_bricks(a, v), tf_s, dtf_s, nf, wk.x, ck,
+                                                      tv.final_rgba[wk.x], tv.dl_drgba[wk.x]);
+      } else {
+        const uint2 wk = a.one.work[item];
+        const Checkpoint ck = a.one.ckpt[(size_t)wk.x * a.one.ckpt_cap + wk.y];
+        nsamp += backward_item<WITH_TF, WITH_DENSITY>(a, v1, rb1, tf_s, dtf_s, nf, wk.x, ck, a.one.final_rgba[wk.x],
+                                                      a.one.dl_drgba[wk.x]);
       }
     }
   }
@@ -594,12 +649,10 @@ size_t backward_smem(int n_tf, bool with_tf) {
 
 }  // namespace
 
-cudaError_t launch_forward_train(const TrainArgs& a, int view, int width, int height, int max_grid, cudaStream_t s) {
-  const int slots = ring_slots(width, height, 8, 4);
-  int grid = (slots + 3) / 4;
-  if (grid > max_grid) grid = max_grid;
+cudaError_t launch_forward_train(const TrainArgs& a, unsigned items, int max_grid, cudaStream_t s) {
+  int grid = (int)std::min<unsigned>((items + 3) / 4, (unsigned)max_grid);
   if (grid < 1) grid = 1;
-  forward_train_kernel<<<grid, 128, (size_t)(a.n_tf + 4) * sizeof(float4), s>>>(a, view);
+  forward_train_kernel<<<grid, 128, (size_t)(a.n_tf + 4) * sizeof(float4), s>>>(a, items);
   return cudaGetLastError();
 }
 
@@ -613,17 +666,21 @@ int forward_train_blocks_per_sm(int n_tf) {
   return n;
 }
 
-cudaError_t launch_backward(const TrainArgs& a, int view, int grid, cudaStream_t s) {
+cudaError_t launch_backward(const TrainArgs& a, int grid, cudaStream_t s) {
   const bool with_tf = a.dtf != nullptr, with_density = a.dgrid4 != nullptr;
   if (!with_tf && !with_density) return cudaErrorInvalidValue;
   const size_t smem = backward_smem(a.n_tf, with_tf);
-  void (*k)(TrainArgs, int) = !with_tf ? backward_kernel<false, true>
-                                       : (with_density ? backward_kernel<true, true> : backward_kernel<true, false>);
+  const bool multi = a.n_views > 1;
+  void (*k)(TrainArgs) =
+      multi ? (!with_tf ? backward_kernel<false, true, true>
+                        : (with_density ? backward_kernel<true, true, true> : backward_kernel<true, false, true>))
+            : (!with_tf ? backward_kernel<false, true, false>
+                        : (with_density ? backward_kernel<true, true, false> : backward_kernel<true, false, false>));
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  k<<<grid, 128, smem, s>>>(a, view);
+  k<<<grid, 128, smem, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -640,13 +697,13 @@ int backward_blocks_per_sm(int n_tf) {
   // the instance with the transfer-function gradient needs more shared memory
   const size_t smem = backward_smem(n_tf, true);
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(backward_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaFuncSetAttribute(backward_kernel<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, backward_kernel<true, true>, 128, smem) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, backward_kernel<true, true, true>, 128, smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }

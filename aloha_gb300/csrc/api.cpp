@@ -137,6 +137,7 @@ struct aloha_ctx {
   // params, scratch
   aloha_render_params params;
   DeviceBuffer counter, flag, staging_out, work, grad4;
+  DeviceBuffer train_tables;  // per launch of the differentiable form: item counter, views, runs
   // persistent render of one view: chunk shape and grid (occupancy depends on
   // the transfer-function size through shared memory)
   int chunk_w = 0, chunk_h = 0;  // 0 = automatic
@@ -1223,7 +1224,7 @@ unsigned checkpoint_capacity(const aloha_ctx* c, unsigned k) {
   return (unsigned)std::ceil(bound / k) + 1;
 }
 
-TrainArgs train_args(aloha_ctx* c, TrainState& t) {
+TrainArgs train_args(aloha_ctx* c) {
   const aloha_render_params& p = c->params;
   TrainArgs a{};
   a.bricks = static_cast<const DevBrick*>(c->bricks_dev.ptr);
@@ -1236,16 +1237,163 @@ TrainArgs train_args(aloha_ctx* c, TrainState& t) {
   a.jitter_mode = p.jitter_mode;
   a.jitter_value = p.jitter_value;
   a.accum_id = p.accum_id;
-  a.k = t.k;
-  a.ckpt_cap = t.cap;
-  a.ckpt = t.ckpt;
-  a.final_rgba = t.final_rgba;
-  a.work = t.work;
-  a.work_cap = (unsigned)std::min<size_t>(t.npx * t.cap, 0xffffffffu);
-  a.work_count = t.work_count;
-  a.overflow = t.overflow;
   a.counter = static_cast<unsigned long long*>(c->counter.ptr);
   return a;
+}
+
+TrainView train_view(const TrainState& t, int view) {
+  TrainView tv{};
+  tv.ckpt = t.ckpt;
+  tv.final_rgba = t.final_rgba;
+  tv.work = t.work;
+  tv.work_count = t.work_count;
+  tv.overflow = t.overflow;
+  tv.ckpt_cap = t.cap;
+  tv.work_cap = (unsigned)std::min<size_t>(t.npx * t.cap, 0xffffffffu);
+  tv.view = view;
+  return tv;
+}
+
+// Uploads a launch's tables (one block: the item counter, zeroed, then the
+// parts at 16-byte aligned offsets) and returns their device addresses.
+int upload_train_tables(aloha_ctx* c, const std::vector<std::pair<const void*, size_t>>& parts, cudaStream_t s,
+                        std::vector<char*>& dev) {
+  std::vector<size_t> off(parts.size());
+  size_t total = 16;
+  for (size_t i = 0; i < parts.size(); ++i) {
+    off[i] = total;
+    total += (parts[i].second + 15) & ~(size_t)15;
+  }
+  std::vector<char> host(total, 0);
+  for (size_t i = 0; i < parts.size(); ++i)
+    if (parts[i].second) std::memcpy(host.data() + off[i], parts[i].first, parts[i].second);
+  CUDA_TRY(c, c->train_tables.ensure(total));
+  char* base = static_cast<char*>(c->train_tables.ptr);
+  // pageable source: staged by the runtime before the call returns
+  CUDA_TRY(c, cudaMemcpyAsync(base, host.data(), total, cudaMemcpyHostToDevice, s));
+  dev.assign(parts.size() + 1, nullptr);
+  dev[0] = base;
+  for (size_t i = 0; i < parts.size(); ++i) dev[i + 1] = base + off[i];
+  return ALOHA_OK;
+}
+
+// The training forward of several views in one persistent launch: each
+// view's checkpoints, final colour and segment list as aloha_forward keeps
+// them.  One view keeps its cost-ordered chunks (frames of 512^2 and up);
+// several march their chunks centre-out, position-major across the views.
+int forward_views(aloha_ctx* c, int n_views, const int* view_ids, float* const* rgba, int checkpoint_every,
+                  void* stream) {
+  if (!c) return ALOHA_ERR_NULL_POINTER;
+  if (n_views < 1) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "no views");
+  if (!view_ids || !rgba) return c->fail(ALOHA_ERR_NULL_POINTER, "no view list");
+  if (checkpoint_every < 1 || checkpoint_every > 65535)
+    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "checkpoint_every %d not in [1, 65535]", checkpoint_every);
+  for (int i = 0; i < n_views; ++i) {
+    if (!rgba[i]) return c->fail(ALOHA_ERR_NULL_POINTER, "no image for view %d", view_ids[i]);
+    for (int j = 0; j < i; ++j)
+      if (view_ids[j] == view_ids[i]) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "view %d given twice", view_ids[i]);
+  }
+  int rc = check_trainable(c);
+  if (rc) return rc;
+  if ((int)c->descs.size() > 65535) return c->fail(ALOHA_ERR_UNSUPPORTED, "more than 65535 bricks");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  const unsigned k = (unsigned)checkpoint_every;
+  const unsigned cap = checkpoint_capacity(c, k);
+  std::vector<TrainView> tvs(n_views);
+  std::vector<char> host_out(n_views, 0);
+  for (int i = 0; i < n_views; ++i) {
+    const int view = view_ids[i];
+    rc = prepare_view(c, view, s);
+    if (rc) return rc;
+    ViewState& v = c->views[view];
+    TrainState& t = v.train;
+    t.valid = false;
+    const size_t npx = (size_t)v.width * v.height;
+    if (npx * cap > 0xffffffffull)
+      return c->fail(ALOHA_ERR_UNSUPPORTED, "too many checkpoint segments for view %d", view);
+    const size_t need = npx * cap * (sizeof(Checkpoint) + sizeof(uint2)) + npx * sizeof(float4);
+    if (t.npx != npx || t.cap != cap) {
+      CUDA_TRY(c, cudaStreamSynchronize(s));
+      t.release();
+      size_t free_b = 0, total_b = 0;
+      CUDA_TRY(c, cudaMemGetInfo(&free_b, &total_b));
+      if (need > free_b)
+        return c->fail(ALOHA_ERR_OUT_OF_MEMORY, "checkpoints of view %d need %zu bytes, %zu free", view, need, free_b);
+      CUDA_TRY(c, cudaMalloc(&t.ckpt, npx * cap * sizeof(Checkpoint)));
+      CUDA_TRY(c, cudaMalloc(&t.work, npx * cap * sizeof(uint2)));
+      CUDA_TRY(c, cudaMalloc(&t.final_rgba, npx * sizeof(float4)));
+      CUDA_TRY(c, cudaMalloc(&t.work_count, 4 * sizeof(unsigned)));
+      CUDA_TRY(c, cudaMalloc(&t.overflow, sizeof(int)));
+      t.npx = npx;
+      t.cap = cap;
+      t.bytes = need;
+    }
+    t.k = k;
+    tvs[i] = train_view(t, view);
+    host_out[i] = !is_device_pointer(rgba[i]);
+    tvs[i].out_rgba = host_out[i] ? nullptr : reinterpret_cast<float4*>(rgba[i]);
+    CUDA_TRY(c, cudaMemsetAsync(t.work_count, 0, 4 * sizeof(unsigned), s));
+    CUDA_TRY(c, cudaMemsetAsync(t.overflow, 0, sizeof(int), s));
+    tvs[i].n_chunks = ring_slots(v.width, v.height, 8, 4);
+  }
+  if (n_views == 1) {
+    const int* order = nullptr;
+    int chunks = 0;
+    rc = plan_chunk_order(c, frame_args(c), view_ids[0], 8, 4, s, &order, &chunks);
+    if (rc) return rc;
+    if (order) {
+      tvs[0].chunk_order = order;
+      tvs[0].n_chunks = chunks;
+    }
+  }
+  // position-major runs over the views sorted by positions, descending
+  std::vector<int> by_size(n_views);
+  for (int i = 0; i < n_views; ++i) by_size[i] = i;
+  std::stable_sort(by_size.begin(), by_size.end(),
+                   [&](int x, int y) { return tvs[x].n_chunks > tvs[y].n_chunks; });
+  std::vector<TrainRun> runs;
+  unsigned long long items = 0;
+  int p = 0;
+  for (int active = n_views; active > 0; --active) {
+    const int p_end = tvs[by_size[active - 1]].n_chunks;  // views [0, active) have positions below p_end
+    if (p_end <= p) continue;
+    runs.push_back(TrainRun{p, active, (unsigned)items, 0u});
+    items += (unsigned long long)(p_end - p) * (unsigned)active;
+    p = p_end;
+  }
+  if (items >= 0xffffffffull) return c->fail(ALOHA_ERR_UNSUPPORTED, "too many chunks in one training forward");
+  const int n_runs = (int)runs.size();
+  runs.push_back(TrainRun{p, 1, (unsigned)items, 0u});
+  std::vector<char*> dev;
+  rc = upload_train_tables(c, {{tvs.data(), tvs.size() * sizeof(TrainView)},
+                               {runs.data(), runs.size() * sizeof(TrainRun)},
+                               {by_size.data(), by_size.size() * sizeof(int)}}, s, dev);
+  if (rc) return rc;
+  TrainArgs a = train_args(c);
+  a.k = k;
+  a.grab = reinterpret_cast<unsigned*>(dev[0]);
+  a.tv = reinterpret_cast<const TrainView*>(dev[1]);
+  a.n_views = n_views;
+  a.runs = reinterpret_cast<const TrainRun*>(dev[2]);
+  a.n_runs = n_runs;
+  a.run_views = reinterpret_cast<const int*>(dev[3]);
+  CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
+  const int per_sm = forward_train_blocks_per_sm(c->n_tf);
+  if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "forward occupancy query failed");
+  CUDA_TRY(c, launch_forward_train(a, (unsigned)items, per_sm * c->num_sms, s));
+  c->samples_valid = true;
+  bool any_host = false;
+  for (int i = 0; i < n_views; ++i) {
+    TrainState& t = c->views[view_ids[i]].train;
+    t.valid = true;
+    if (host_out[i]) {
+      CUDA_TRY(c, cudaMemcpyAsync(rgba[i], t.final_rgba, t.npx * sizeof(float4), cudaMemcpyDeviceToHost, s));
+      any_host = true;
+    }
+  }
+  if (any_host) CUDA_TRY(c, cudaStreamSynchronize(s));
+  return ALOHA_OK;
 }
 
 // The backward of several views into one pair of gradients: the views'
@@ -1289,16 +1437,24 @@ int backward_views(aloha_ctx* c, int n_views, const int* view_ids, const float* 
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   CUDA_TRY(c, cudaSetDevice(c->device));
-  {
-    // every view's overflow flag, read with one wait
-    std::vector<int> overflow(n_views, 0);
-    for (int i = 0; i < n_views; ++i)
-      CUDA_TRY(c, cudaMemcpyAsync(&overflow[i], c->views[view_ids[i]].train.overflow, sizeof(int),
-                                  cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(c, cudaStreamSynchronize(s));
-    for (int i = 0; i < n_views; ++i)
-      if (overflow[i])
-        return c->fail(ALOHA_ERR_OUT_OF_RANGE, "a ray of view %d needed more checkpoints than reserved", view_ids[i]);
+  // every view's overflow flag and segment count, read with one wait
+  std::vector<int> overflow(n_views, 0);
+  std::vector<unsigned> segments(n_views, 0);
+  for (int i = 0; i < n_views; ++i) {
+    const TrainState& t = c->views[view_ids[i]].train;
+    CUDA_TRY(c, cudaMemcpyAsync(&overflow[i], t.overflow, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(c, cudaMemcpyAsync(&segments[i], t.work_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(s));
+  std::vector<unsigned> item_base(n_views + 1, 0);
+  for (int i = 0; i < n_views; ++i) {
+    if (overflow[i])
+      return c->fail(ALOHA_ERR_OUT_OF_RANGE, "a ray of view %d needed more checkpoints than reserved", view_ids[i]);
+    const TrainState& t = c->views[view_ids[i]].train;
+    const unsigned long long n = std::min<unsigned long long>(segments[i], t.npx * t.cap);
+    if (item_base[i] + n >= 0xffffffffull)
+      return c->fail(ALOHA_ERR_UNSUPPORTED, "too many checkpoint segments in one backward");
+    item_base[i + 1] = item_base[i] + (unsigned)n;
   }
   const size_t tf_bytes = (size_t)c->n_tf * 4 * sizeof(float), g_bytes = grid_elems * sizeof(float);
   const bool h_tf = dl_dtf && !is_device_pointer(dl_dtf), h_grid = with_density && !is_device_pointer(dl_ddensity);
@@ -1336,18 +1492,57 @@ int backward_views(aloha_ctx* c, int n_views, const int* view_ids, const float* 
   const int per_sm = backward_blocks_per_sm(c->n_tf);
   if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "backward occupancy query failed");
   CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
-  for (int i = 0; i < n_views; ++i) {
-    TrainState& t = c->views[view_ids[i]].train;
-    TrainArgs a = train_args(c, t);
-    a.dl_drgba = off_dl[i] != SIZE_MAX ? reinterpret_cast<const float4*>(st + off_dl[i])
-                                       : reinterpret_cast<const float4*>(dl_drgba[i]);
+  // one launch per checkpoint interval among the views (the interval is a
+  // launch constant of the replay loop), all into the same gradients
+  std::vector<char> done(n_views, 0);
+  for (int first = 0; first < n_views; ++first) {
+    if (done[first]) continue;
+    const unsigned k = c->views[view_ids[first]].train.k;
+    std::vector<TrainView> tvs;
+    std::vector<unsigned> base{0};
+    for (int i = first; i < n_views; ++i) {
+      if (done[i] || c->views[view_ids[i]].train.k != k) continue;
+      done[i] = 1;
+      TrainView tv = train_view(c->views[view_ids[i]].train, view_ids[i]);
+      tv.dl_drgba = off_dl[i] != SIZE_MAX ? reinterpret_cast<const float4*>(st + off_dl[i])
+                                          : reinterpret_cast<const float4*>(dl_drgba[i]);
+      tvs.push_back(tv);
+      base.push_back(base.back() + (item_base[i + 1] - item_base[i]));
+    }
+    std::vector<char*> dev;
+    rc = upload_train_tables(c, {{tvs.data(), tvs.size() * sizeof(TrainView)},
+                                 {base.data(), base.size() * sizeof(unsigned)}}, s, dev);
+    if (rc) return rc;
+    TrainArgs a = train_args(c);
+    a.k = k;
+    a.grab = reinterpret_cast<unsigned*>(dev[0]);
     a.dtf = dtf;
     a.dgrid4 = dgrid4;
     a.brick_grid_origin = reinterpret_cast<const int4*>(st + off_org);
     if (with_density)
-      for (int k = 0; k < 3; ++k) a.grid_dims[k] = grid_dims[k];
-    CUDA_TRY(c, cudaMemsetAsync(a.work_count + 2, 0, sizeof(unsigned), s));  // the backward's grab counter
-    CUDA_TRY(c, launch_backward(a, view_ids[i], c->num_sms * per_sm, s));
+      for (int d = 0; d < 3; ++d) a.grid_dims[d] = grid_dims[d];
+    // Views whose items give every resident thread many of them fill the GPU
+    // alone: one launch each, with the view in the launch parameters (the
+    // replay's registers then hold no per-view pointers).  Smaller views go
+    // together into one launch, which fills the GPU with all of them.
+    const unsigned long long resident = (unsigned long long)c->num_sms * per_sm * 128;
+    bool all_large = true;
+    for (size_t i = 0; i + 1 < base.size(); ++i)
+      if ((unsigned long long)(base[i + 1] - base[i]) < 16 * resident) all_large = false;
+    if (tvs.size() == 1 || all_large) {
+      for (size_t i = 0; i < tvs.size(); ++i) {
+        if (i > 0) CUDA_TRY(c, cudaMemsetAsync(a.grab, 0, sizeof(unsigned), s));
+        a.n_views = 1;
+        a.one = tvs[i];
+        a.one_items = base[i + 1] - base[i];
+        CUDA_TRY(c, launch_backward(a, c->num_sms * per_sm, s));
+      }
+    } else {
+      a.tv = reinterpret_cast<const TrainView*>(dev[1]);
+      a.n_views = (int)tvs.size();
+      a.item_base = reinterpret_cast<const unsigned*>(dev[2]);
+      CUDA_TRY(c, launch_backward(a, c->num_sms * per_sm, s));
+    }
   }
   if (with_density) CUDA_TRY(c, launch_fold_quads(dgrid4, grid_out, grid_dims, s));
   c->samples_valid = true;
@@ -1363,56 +1558,12 @@ extern "C" {
 
 int aloha_forward(aloha_ctx* c, int view, float* rgba, int checkpoint_every, void* stream) {
   if (!c || !rgba) return ALOHA_ERR_NULL_POINTER;
-  if (checkpoint_every < 1 || checkpoint_every > 65535)
-    return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "checkpoint_every %d not in [1, 65535]", checkpoint_every);
-  int rc = check_trainable(c);
-  if (rc) return rc;
-  if ((int)c->descs.size() > 65535) return c->fail(ALOHA_ERR_UNSUPPORTED, "more than 65535 bricks");
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  CUDA_TRY(c, cudaSetDevice(c->device));
-  rc = prepare_view(c, view, s);
-  if (rc) return rc;
-  ViewState& v = c->views[view];
-  TrainState& t = v.train;
-  const size_t npx = (size_t)v.width * v.height;
-  const unsigned k = (unsigned)checkpoint_every;
-  const unsigned cap = checkpoint_capacity(c, k);
-  if (npx * cap > 0xffffffffull) return c->fail(ALOHA_ERR_UNSUPPORTED, "too many checkpoint segments for one view");
-  const size_t need = npx * cap * (sizeof(Checkpoint) + sizeof(uint2)) + npx * sizeof(float4);
-  if (t.npx != npx || t.cap != cap) {
-    CUDA_TRY(c, cudaStreamSynchronize(s));
-    t.release();
-    size_t free_b = 0, total_b = 0;
-    CUDA_TRY(c, cudaMemGetInfo(&free_b, &total_b));
-    if (need > free_b)
-      return c->fail(ALOHA_ERR_OUT_OF_MEMORY, "checkpoints need %zu bytes, %zu free", need, free_b);
-    CUDA_TRY(c, cudaMalloc(&t.ckpt, npx * cap * sizeof(Checkpoint)));
-    CUDA_TRY(c, cudaMalloc(&t.work, npx * cap * sizeof(uint2)));
-    CUDA_TRY(c, cudaMalloc(&t.final_rgba, npx * sizeof(float4)));
-    CUDA_TRY(c, cudaMalloc(&t.work_count, 4 * sizeof(unsigned)));
-    CUDA_TRY(c, cudaMalloc(&t.overflow, sizeof(int)));
-    t.npx = npx;
-    t.cap = cap;
-    t.bytes = need;
-  }
-  t.k = k;
-  TrainArgs a = train_args(c, t);
-  const bool host = !is_device_pointer(rgba);
-  a.out_rgba = host ? nullptr : reinterpret_cast<float4*>(rgba);
-  CUDA_TRY(c, cudaMemsetAsync(t.work_count, 0, 4 * sizeof(unsigned), s));
-  CUDA_TRY(c, cudaMemsetAsync(t.overflow, 0, sizeof(int), s));
-  CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
-  const int per_sm = forward_train_blocks_per_sm(c->n_tf);
-  if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "forward occupancy query failed");
-  {
-    const int rc = plan_chunk_order(c, frame_args(c), view, 8, 4, s, &a.chunk_order, &a.n_chunks);
-    if (rc) return rc;
-  }
-  CUDA_TRY(c, launch_forward_train(a, view, v.width, v.height, per_sm * c->num_sms, s));
-  c->samples_valid = true;
-  t.valid = true;
-  if (host) return finish_host_output(c, rgba, t.final_rgba, npx * sizeof(float4), s);
-  return ALOHA_OK;
+  return forward_views(c, 1, &view, &rgba, checkpoint_every, stream);
+}
+
+int aloha_forward_views(aloha_ctx* c, int n_views, const int* views, float* const* rgba, int checkpoint_every,
+                        void* stream) {
+  return forward_views(c, n_views, views, rgba, checkpoint_every, stream);
 }
 
 int aloha_backward(aloha_ctx* c, int view, const float* dl_drgba, float* dl_dtf, float* dl_ddensity,

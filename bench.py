@@ -550,7 +550,10 @@ def adjoint_section(name, vol, descs, cams, W, H, k, stream, dev):
     dtf = torch.zeros((256, 4), dtype=torch.float32, device=dev)
     dden = torch.zeros(tuple(vol.shape), dtype=torch.float32, device=dev)
 
-    def fwd():
+    def fwd(batched=False):
+        if batched:  # all views in one aloha_forward_views launch
+            ctx.forward_views(list(range(nv)), [img[v] for v in range(nv)], k, stream)
+            return
         for v in range(nv):
             ctx.forward(v, img[v], k, stream)
 
@@ -609,18 +612,20 @@ def adjoint_section(name, vol, descs, cams, W, H, k, stream, dev):
         e[2].record(stream)
         torch.cuda.synchronize()
         tf_ms += e[1].elapsed_time(e[2]) / reps
-    # the views' gradients summed by one aloha_backward_views call (one
-    # accumulation buffer cleared and folded once, one host wait)
-    sum_ms, sum_den_ms = 0.0, 0.0
+    # the views in one launch each way: aloha_forward_views, then their
+    # gradients summed by one aloha_backward_views call (one accumulation
+    # buffer cleared and folded once, one host wait, one launch)
+    sum_ms, sum_den_ms, fwdv_ms = 0.0, 0.0, 0.0
     for _ in range(reps):
         for with_tf in (True, False):
             torch.cuda.synchronize()
             e[0].record(stream)
-            fwd()
+            fwd(batched=True)
             e[1].record(stream)
             bwd(grad, with_tf=with_tf, summed=True)
             e[2].record(stream)
             torch.cuda.synchronize()
+            fwdv_ms += e[0].elapsed_time(e[1]) / (2 * reps)
             if with_tf:
                 sum_ms += e[1].elapsed_time(e[2]) / reps
             else:
@@ -633,8 +638,10 @@ def adjoint_section(name, vol, descs, cams, W, H, k, stream, dev):
             "fwd_plus_density_adjoint_over_fwd": (fwd_ms + den_ms) / fwd_ms,
             "adjoint_tf_only_ms_per_view": tf_ms / nv,
             "fwd_plus_tf_adjoint_over_fwd": (fwd_ms + tf_ms) / fwd_ms,
+            "fwd_views_ms_per_view": fwdv_ms / nv,
             "adjoint_views_summed_ms_per_view": sum_ms / nv,
             "adjoint_views_summed_density_only_ms_per_view": sum_den_ms / nv,
+            "views_fwd_plus_adjoint_over_fwd": (fwdv_ms + sum_ms) / fwdv_ms,
             "samples_per_view": samples / nv,
             "fwd_gsamples_per_s": samples / (fwd_ms * 1e-3) / 1e9,
             "fwd_plus_adjoint_gsamples_per_s": samples / ((fwd_ms + bwd_ms) * 1e-3) / 1e9}

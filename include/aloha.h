@@ -281,6 +281,15 @@ int aloha_render_batch(aloha_ctx* ctx, const int* views, int n_items, uint32_t* 
  * every `checkpoint_every` samples for the view's next aloha_backward. */
 int aloha_forward(aloha_ctx* ctx, int view, float* rgba, int checkpoint_every, void* stream);
 
+/* aloha_forward of views[0..n_views) in one persistent launch: rgba[i]
+ * receives views[i]'s image (host or device), and each view keeps the
+ * checkpoints its aloha_backward / aloha_backward_views needs; images and
+ * checkpoints are those of n aloha_forward calls, bit for bit.  Each view at
+ * most once.  Views small enough to leave part of the GPU idle (a 256^2 frame
+ * has fewer 8x4 chunks than a GB300 holds warps) gain most. */
+int aloha_forward_views(aloha_ctx* ctx, int n_views, const int* views, float* const* rgba, int checkpoint_every,
+                        void* stream);
+
 /* Gradient of a loss L with respect to the transfer function and the voxel
  * densities, given dL/dRGBA of the last aloha_forward of `view`
  * ([height][width][4] float).  Accumulates (+=) into dl_dtf ([n_tf][4]) and
@@ -301,8 +310,10 @@ int aloha_backward(aloha_ctx* ctx, int view, const float* dl_drgba, float* dl_dt
  * dL/dRGBA of views[i] (each view at most once, each with a current
  * aloha_forward).  Same arguments and rules as aloha_backward otherwise.  The
  * views' replays accumulate into one device buffer that is cleared and folded
- * into the density grid once, and their checkpoint-overflow flags are read
- * with one host wait, so n views cost less than n calls of aloha_backward.
+ * into the density grid once, their checkpoint-overflow flags are read with
+ * one host wait, and one persistent launch replays every view's segments, so
+ * n views cost less than n calls of aloha_backward.  The views may have been
+ * forwarded with different checkpoint intervals.
  * The sum is taken in a different order than n calls would take it (float
  * atomics), so results agree with those calls to rounding. */
 int aloha_backward_views(aloha_ctx* ctx, int n_views, const int* views, const float* const* dl_drgba,

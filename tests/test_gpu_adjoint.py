@@ -367,6 +367,57 @@ def test_backward_views_is_the_sum(gpu_ctx_factory, oracle, where):
     assert e.value.code == abi.ERR_NOT_READY
 
 
+@pytest.mark.parametrize("bricks", [1, 8])
+def test_forward_views_equals_single_forwards(gpu_ctx_factory, oracle, bricks):
+    """aloha_forward_views renders every view's image bit for bit as
+    aloha_forward does (host and device images, different sizes, centre-out
+    chunks across views), and leaves checkpoints the backward replays: the
+    summed gradient of views forwarded together, and of views forwarded at two
+    different checkpoint intervals, matches the FP64 oracle."""
+    torch = pytest.importorskip("torch")
+    n = 48
+    vol, descs, vox = density_scene(n, seed=23, bricks=bricks)
+    tf = S.ramp_tf()
+    ctx = setup(gpu_ctx_factory, descs, vox, tf)
+    sizes = {0: (64, 48), 3: (40, 40), 5: (96, 33), 7: (8, 8)}
+    cams = T.cameras((n, n, n), 8, 64, 64, seed=61)
+    ref_img = {}
+    for v, (W, H) in sizes.items():
+        ctx.set_camera(v, *cams[v])
+        ctx.resize(v, W, H)
+        ref = oracle.render(descs, vox, tf, oracle.make_camera(*cams[v]), W, H, oracle.make_params(), n_ranks=1,
+                            want=("final",))
+        ref_img[v] = ref["final"]
+    views = [5, 0, 7, 3]
+    imgs = [np.zeros((sizes[v][1], sizes[v][0], 4), np.float32) if i % 2 else
+            torch.zeros((sizes[v][1], sizes[v][0], 4), device="cuda") for i, v in enumerate(views)]
+    ctx.forward_views(views, imgs, 16)
+    torch.cuda.synchronize()
+    for v, img in zip(views, imgs):
+        got = img.cpu().numpy() if hasattr(img, "cpu") else img
+        np.testing.assert_array_equal(got, ref_img[v])
+    rng = np.random.default_rng(3)
+    dls = [rng.uniform(-1, 1, (sizes[v][1], sizes[v][0], 4)).astype(np.float32) for v in views]
+    ref_tf = np.zeros((tf.shape[0], 4))
+    ref_den = np.zeros((n, n, n))
+    for v, dl in zip(views, dls):
+        W, H = sizes[v]
+        r = oracle.adjoint(descs, vox, tf, oracle.make_camera(*cams[v]), W, H, dl, (0, 0, 0), (n, n, n))
+        ref_tf += r["dtf"]
+        ref_den += r["ddensity"]
+    for mixed in (False, True):
+        if mixed:  # views 0 and 3 again, at another interval: two replay launches
+            ctx.forward_views([0, 3], [np.zeros((sizes[v][1], sizes[v][0], 4), np.float32) for v in (0, 3)], 7)
+        dtf = np.zeros((tf.shape[0], 4), np.float32)
+        dden = np.zeros((n, n, n), np.float32)
+        ctx.backward_views(views, dls, dtf, dden, (0, 0, 0), (n, n, n))
+        assert rel_err(dtf, ref_tf) < 2e-3, mixed
+        assert rel_err(dden, ref_den) < 2e-3, mixed
+    with pytest.raises(abi.AlohaError) as e:
+        ctx.forward_views([0, 0], [imgs[1], imgs[1]], 16)
+    assert e.value.code == abi.ERR_INVALID_ARGUMENT
+
+
 def test_autograd_gradient_flags_and_uploads(gpu_ctx_factory):
     """The binding computes only the gradients autograd asks for, and uploads
     the bricks again only when the density tensor changed."""
