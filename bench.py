@@ -849,11 +849,20 @@ def large_section(dev, n=1024, size=2048, views=8, k=64):
     fwd_ms = timed(fwd) / views
     bwd_ms = timed(bwd) / views
     den_ms = timed(lambda: bwd(False)) / views
+    # the batch as the configuration states it: all views' forwards in one
+    # launch, their gradients summed by one call
+    vs = list(range(views))
+    fwdv_ms = timed(lambda: ctx.forward_views(vs, [img[v] for v in vs], k, stream)) / views
+    sumv_ms = timed(lambda: ctx.backward_views(vs, [dl] * views, dtf, dden, (0, 0, 0), dims, stream)) / views
+    sumd_ms = timed(lambda: ctx.backward_views(vs, [dl] * views, None, dden, (0, 0, 0), dims, stream)) / views
     ctx.close()
     out.update({"checkpoint_every": k, "fwd_ms_per_view": fwd_ms, "adjoint_ms_per_view": bwd_ms,
                 "fwd_plus_adjoint_over_fwd": (fwd_ms + bwd_ms) / fwd_ms,
                 "adjoint_density_only_ms_per_view": den_ms,
-                "fwd_plus_density_adjoint_over_fwd": (fwd_ms + den_ms) / fwd_ms})
+                "fwd_plus_density_adjoint_over_fwd": (fwd_ms + den_ms) / fwd_ms,
+                "fwd_views_ms_per_view": fwdv_ms, "adjoint_views_summed_ms_per_view": sumv_ms,
+                "adjoint_views_summed_density_only_ms_per_view": sumd_ms,
+                "views_fwd_plus_adjoint_over_fwd": (fwdv_ms + sumv_ms) / fwdv_ms})
     return out
 
 
