@@ -20,8 +20,9 @@ Two more sweeps draw the batched launch (1 to 10 views of random sizes, every
 chunk shape, CTA count and staging, plain or graph launch; each view's frame
 bit-identical to the oracle's) and the differentiable form (random
 single-rank scenes and checkpoint intervals; the training forward's float
-image bit-identical, both gradients within 1e-3 of the FP64 adjoint).  A
-last one drives one context through random call sequences.
+image bit-identical, both gradients within 1e-3 of the FP64 adjoint), the
+multi-view training calls (one forward launch over many views, a summed
+backward), and one context driven through random call sequences.
 """
 import numpy as np
 import pytest
@@ -372,3 +373,71 @@ def test_random_call_sequences(gpu_ctx_factory, oracle, seed):
                             n_ranks=st["n_ranks"], brick_rank=st["brick_rank"], want=("fb",))
         assert np.array_equal(fb, ref["fb"]), f"{where}: {np.count_nonzero(fb != ref['fb'])} pixels differ"
         assert samples == ref["samples"], where
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_multi_view_training(gpu_ctx_factory, oracle, seed):
+    """aloha_forward_views over 2 to 12 views of random sizes (1 to 96 pixels a
+    side) in one launch: every image bit-identical to the oracle's; then
+    aloha_backward_views over them, some re-forwarded at a second checkpoint
+    interval, with a random choice of gradients: the sums within 2e-3 of the
+    FP64 adjoints' sum."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(11000 + seed)
+    dims = tuple(int(x) for x in rng.integers(9, 41, size=3))
+    vol = _volume(rng, dims)
+    descs = _bricks(rng, dims)
+    vox = S.extract_bricks(vol, descs)
+    tf = _tf(rng)
+    params = dict(dt=float(rng.choice([0.5, 1.0, 0.375])), et_alpha=float(rng.choice([0.99, 2.0])),
+                  jitter_mode=int(rng.choice([abi.JITTER_NONE, abi.JITTER_HASH])))
+    ctx = gpu_ctx_factory()
+    ctx.set_bricks(descs, vox)
+    ctx.set_transfer_function(tf)
+    ctx.set_ranks(1)
+    ctx.set_params(**params)
+    op = oracle.make_params(**params)
+    n_views = int(rng.integers(2, 13))
+    views = [int(v) for v in rng.permutation(32)[:n_views]]
+    sizes, cams = {}, {}
+    for v in views:
+        W, H = (int(x) for x in rng.choice([1, 5, 24, 40, 96], p=[.1, .15, .25, .3, .2], size=2))
+        sizes[v] = (W, H)
+        cams[v] = _camera(rng, dims, W, H)
+        ctx.set_camera(v, *cams[v])
+        ctx.resize(v, W, H)
+    k = int(rng.choice([1, 7, 32]))
+    imgs = [np.zeros((sizes[v][1], sizes[v][0], 4), np.float32) if rng.random() < 0.5 else
+            torch.zeros((sizes[v][1], sizes[v][0], 4), device="cuda") for v in views]
+    ctx.forward_views(views, imgs, k)
+    torch.cuda.synchronize()
+    for v, img in zip(views, imgs):
+        W, H = sizes[v]
+        ref = oracle.render(descs, vox, tf, oracle.make_camera(*cams[v]), W, H, op, n_ranks=1, want=("final",))
+        got = img.cpu().numpy() if hasattr(img, "cpu") else img
+        np.testing.assert_array_equal(got, ref["final"], err_msg=f"seed {seed} view {v} {W}x{H}")
+    again = [v for v in views if rng.random() < 0.3]
+    if again:
+        ctx.forward_views(again, [np.zeros((sizes[v][1], sizes[v][0], 4), np.float32) for v in again],
+                          int(rng.choice([3, 16, 64])))
+    nx, ny, nz = dims
+    dls = [rng.uniform(-1, 1, (sizes[v][1], sizes[v][0], 4)).astype(np.float32) for v in views]
+    want_tf, want_den = [(True, True), (True, False), (False, True)][int(rng.integers(0, 3))]
+    dtf = np.zeros((tf.shape[0], 4), np.float32) if want_tf else None
+    dden = np.zeros((nz, ny, nx), np.float32) if want_den else None
+    ctx.backward_views(views, dls, dtf, dden, (0, 0, 0) if want_den else None, (nx, ny, nz) if want_den else None)
+    ref_tf = np.zeros((tf.shape[0], 4))
+    ref_den = np.zeros((nz, ny, nx))
+    for v, dl in zip(views, dls):
+        W, H = sizes[v]
+        r = oracle.adjoint(descs, vox, tf, oracle.make_camera(*cams[v]), W, H, dl, (0, 0, 0), (nx, ny, nz), op)
+        ref_tf += r["dtf"]
+        ref_den += r["ddensity"]
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+    where = f"seed {seed}: {n_views} views, k {k}, re-forwarded {again}, gradients tf {want_tf} density {want_den}"
+    if want_tf and np.linalg.norm(ref_tf) > 0:
+        assert rel(dtf, ref_tf) < 2e-3, where
+    if want_den and np.linalg.norm(ref_den) > 0:
+        assert rel(dden, ref_den) < 2e-3, where
