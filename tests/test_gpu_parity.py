@@ -633,3 +633,60 @@ def test_bricks_that_partitionkd_cannot_split(gpu_ctx_factory, oracle):
     ctx.set_ranks(1)  # one rank always partitions
     fb1, _ = gpu_frame(ctx, cam, W, H)
     assert_same_fb(fb1, oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=1)["fb"])
+
+
+def test_two_contexts_are_independent(gpu_ctx_factory, oracle):
+    """Two contexts on one GPU with different scenes, rank counts, transfer
+    functions and parameters, driven on two CUDA streams at once: renders,
+    a batch and the training forward of one overlap with the other's work,
+    and every result equals the oracle's for its own context."""
+    torch = pytest.importorskip("torch")
+    _, da, va, tfa = T.chopsuey_scene(48, 8, seed=3)
+    _, db, vb, _ = T.uneven_scene(56, seed=4)
+    tfb = S.seeded_tf(19, n=200)
+    A, B = gpu_ctx_factory(), gpu_ctx_factory()
+    A.set_bricks(da, va)
+    A.set_transfer_function(tfa)
+    A.set_ranks(8)
+    B.set_bricks(db, vb)
+    B.set_transfer_function(tfb)
+    B.set_ranks(3)
+    pb = dict(dt=0.3, composite_mode=abi.COMPOSITE_UBYTE, jitter_mode=abi.JITTER_CONST, jitter_value=0.25)
+    A.set_params()
+    B.set_params(**pb)
+    sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
+    W, H = 96, 80
+    cams_a = S.orbit_cameras((48, 48, 48), 4, W, H, seed=5)
+    cams_b = S.orbit_cameras((56, 56, 56), 4, W, H, seed=6)
+    for v in range(4):
+        A.set_camera(v, *cams_a[v])
+        A.resize(v, W, H)
+        B.set_camera(v, *cams_b[v])
+        B.resize(v, W, H)
+    fa = [torch.zeros((H, W), dtype=torch.int32, device="cuda") for _ in range(4)]
+    fb = [torch.zeros((H, W), dtype=torch.int32, device="cuda") for _ in range(4)]
+    batch_b = B.batch([0, 1, 2, 3], fb)
+    torch.cuda.synchronize()
+    for v in range(4):  # A's plain renders on sa overlap B's batch on sb
+        A.render(v, fa[v], sa)
+    batch_b.launch_graph(sb)
+    torch.cuda.synchronize()
+    for v in range(4):
+        ra = oracle.render(da, va, tfa, oracle.make_camera(*cams_a[v]), W, H, oracle.make_params(), n_ranks=8)
+        rb = oracle.render(db, vb, tfb, oracle.make_camera(*cams_b[v]), W, H, oracle.make_params(**pb), n_ranks=3)
+        assert_same_fb(fa[v].cpu().numpy().view(np.uint32), ra["fb"])
+        assert_same_fb(fb[v].cpu().numpy().view(np.uint32), rb["fb"])
+    batch_b.close()
+    # A's training forward on sa while B renders on sb
+    A.set_ranks(1)
+    imgs = [torch.zeros((H, W, 4), device="cuda") for _ in range(4)]
+    A.forward_views([0, 1, 2, 3], imgs, 16, sa)
+    for v in range(4):
+        B.render(v, fb[v], sb)
+    torch.cuda.synchronize()
+    for v in range(4):
+        ra = oracle.render(da, va, tfa, oracle.make_camera(*cams_a[v]), W, H, oracle.make_params(), n_ranks=1,
+                           want=("final",))
+        np.testing.assert_array_equal(imgs[v].cpu().numpy(), ra["final"])
+        rb = oracle.render(db, vb, tfb, oracle.make_camera(*cams_b[v]), W, H, oracle.make_params(**pb), n_ranks=3)
+        assert_same_fb(fb[v].cpu().numpy().view(np.uint32), rb["fb"])
