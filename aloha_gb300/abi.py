@@ -38,7 +38,7 @@ EXPORTS = [
     "aloha_batch_autotune", "aloha_batch_destroy", "aloha_render_batch", "aloha_forward", "aloha_backward",
     "aloha_composite_over_noalloc", "aloha_set_render_tile", "aloha_set_render_split", "aloha_set_chunk_order",
     "aloha_set_render_staging", "aloha_batch_set_staging", "aloha_batch_get_staging", "aloha_set_lane_groups",
-    "aloha_backward_views", "aloha_forward_views",
+    "aloha_backward_views", "aloha_forward_views", "aloha_batch_set_unroll", "aloha_batch_get_unroll",
 ]
 
 
@@ -106,6 +106,8 @@ _SIGS = {
     "aloha_backward": ([P, I, P, P, P, P, P, P], I),
     "aloha_backward_views": ([P, I, P, P, P, P, P, P, P], I),
     "aloha_forward_views": ([P, I, P, P, I, P], I),
+    "aloha_batch_set_unroll": ([P, I], I),
+    "aloha_batch_get_unroll": ([P, ctypes.POINTER(I)], I),
     "aloha_composite_over_noalloc": ([P, P, I, I, I, I, P, P], I),
     "aloha_set_render_tile": ([P, I, I], I),
     "aloha_set_render_split": ([P, I], I),
@@ -376,6 +378,15 @@ class Batch:
     def staging(self) -> int:
         s = I()
         self.ctx._check(self.ctx._lib.aloha_batch_get_staging(self.h, ctypes.byref(s)))
+        return s.value
+
+    def set_unroll(self, steps: int):
+        """March steps per loop trip: 1 or 2 (direct loads only)."""
+        self.ctx._check(self.ctx._lib.aloha_batch_set_unroll(self.h, int(steps)))
+
+    def unroll(self) -> int:
+        s = I()
+        self.ctx._check(self.ctx._lib.aloha_batch_get_unroll(self.h, ctypes.byref(s)))
         return s.value
 
     def launch(self, stream=None):

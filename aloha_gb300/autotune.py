@@ -1,9 +1,10 @@
 """Autotuner of the batched render with a JSON cache.
 
 The persistent batched kernel comes in four ray-tile shapes (8x4, 8x8, 16x8
-and 32x4 pixels per warp chunk), each with direct stencil loads or with the
-next sample's stencil rows staged in shared memory; ``aloha_batch_autotune``
-times all eight on the batch itself with CUDA events and keeps the fastest.
+and 32x4 pixels per warp chunk), each with direct stencil loads, direct loads
+with the march loop written out two steps per trip, or the next sample's
+stencil rows staged in shared memory; ``aloha_batch_autotune`` times all
+twelve on the batch itself with CUDA events and keeps the fastest.
 This module caches that choice per (GPU, batch configuration) in a JSON file
 so later processes skip the sweep.
 """
@@ -39,16 +40,17 @@ def _load(path: str) -> dict:
 
 
 def tune(batch, key: str, stream=None, reps: int = 2, path: str | None = None) -> dict:
-    """Apply the cached tile shape and staging for `key`, or sweep, apply and cache them."""
+    """Apply the cached tile shape, staging and unroll for `key`, or sweep, apply and cache them."""
     path = path or cache_path()
     with _LOCK:
         entry = _load(path).get(key)
     if entry:
         batch.set_staging(entry.get("staging", 0))
+        batch.set_unroll(entry.get("unroll", 1))
         batch.set_config(entry["tile_w"], entry["tile_h"], 0)
         return dict(entry, cached=True)
     w, h, ms = batch.autotune(stream, reps=reps)
-    entry = {"tile_w": w, "tile_h": h, "staging": batch.staging(), "ms": ms}
+    entry = {"tile_w": w, "tile_h": h, "staging": batch.staging(), "unroll": batch.unroll(), "ms": ms}
     with _LOCK:
         data = _load(path)
         data[key] = entry

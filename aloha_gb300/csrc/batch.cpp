@@ -17,6 +17,7 @@ struct aloha_batch {
   std::vector<uint32_t*> fbs;
   int tile_w = 16, tile_h = 8, ctas_per_sm = 0;
   int stage = ALOHA_STAGING_NONE;
+  int steps = 1;  // march steps per loop trip (2 only with direct loads)
   int* d_view_ids = nullptr;
   uint32_t** d_fbs = nullptr;
   int* d_prefix = nullptr;
@@ -37,6 +38,12 @@ void drop_graph(aloha_batch* b) {
   b->graph = nullptr;
 }
 
+// The render kernel's stage for the batch's staging and unroll settings
+// (two steps per trip exist for direct loads only).
+int kernel_stage(const aloha_batch* b) {
+  return b->stage == ALOHA_STAGING_NONE && b->steps == 2 ? kStageUnroll2 : b->stage;
+}
+
 // Tile prefix sums and the grid for the current tile shape.
 int configure(aloha_batch* b) {
   aloha_ctx* c = b->ctx;
@@ -50,7 +57,7 @@ int configure(aloha_batch* b) {
   b->total_tiles = prefix.back();
   if (cudaMemcpy(b->d_prefix, prefix.data(), sizeof(int) * prefix.size(), cudaMemcpyHostToDevice) != cudaSuccess)
     return ctx_fail(c, ALOHA_ERR_CUDA, "batch: uploading tile prefix failed");
-  int per_sm = render_blocks_per_sm(b->tile_w, b->tile_h, ctx_n_tf(c), true, b->stage);
+  int per_sm = render_blocks_per_sm(b->tile_w, b->tile_h, ctx_n_tf(c), true, kernel_stage(b));
   if (per_sm <= 0) return ctx_fail(c, ALOHA_ERR_CUDA, "batch: occupancy query failed");
   if (b->ctas_per_sm > 0 && b->ctas_per_sm < per_sm) per_sm = b->ctas_per_sm;
   b->grid = ctx_num_sms(c) * per_sm;
@@ -71,7 +78,7 @@ int enqueue(aloha_batch* b, cudaStream_t s) {
   if (cudaMemsetAsync(b->d_work, 0, sizeof(unsigned int), s) != cudaSuccess ||
       cudaMemsetAsync(a.f.counter, 0, sizeof(unsigned long long), s) != cudaSuccess)
     return ctx_fail(c, ALOHA_ERR_CUDA, "batch: memset failed");
-  cudaError_t e = launch_render_warps(a, b->tile_w, b->tile_h, b->grid, true, s, b->stage);
+  cudaError_t e = launch_render_warps(a, b->tile_w, b->tile_h, b->grid, true, s, kernel_stage(b));
   if (e != cudaSuccess) return ctx_fail(c, ALOHA_ERR_CUDA, "batch launch: %s", cudaGetErrorString(e));
   ctx_mark_samples(c);
   return ALOHA_OK;
@@ -153,6 +160,19 @@ int aloha_batch_get_staging(const aloha_batch* b, int* stage) {
   return ALOHA_OK;
 }
 
+int aloha_batch_set_unroll(aloha_batch* b, int steps) {
+  if (!b) return ALOHA_ERR_NULL_POINTER;
+  if (steps != 1 && steps != 2) return ctx_fail(b->ctx, ALOHA_ERR_INVALID_ARGUMENT, "unroll %d not 1 or 2", steps);
+  b->steps = steps;
+  return configure(b);
+}
+
+int aloha_batch_get_unroll(const aloha_batch* b, int* steps) {
+  if (!b || !steps) return ALOHA_ERR_NULL_POINTER;
+  *steps = b->steps;
+  return ALOHA_OK;
+}
+
 int aloha_batch_get_config(const aloha_batch* b, int* tile_w, int* tile_h, int* ctas_per_sm) {
   if (!b || !tile_w || !tile_h || !ctas_per_sm) return ALOHA_ERR_NULL_POINTER;
   *tile_w = b->tile_w;
@@ -210,13 +230,16 @@ int aloha_batch_autotune(aloha_batch* b, void* stream, int reps, int* tile_w, in
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     return ctx_fail(b->ctx, ALOHA_ERR_CUDA, "cudaEventCreate failed");
+  // the loads and loop forms: direct, direct two steps per trip, staged
+  static const int forms[3][2] = {{ALOHA_STAGING_NONE, 1}, {ALOHA_STAGING_NONE, 2}, {ALOHA_STAGING_NEXT_SAMPLE, 1}};
   float best = -1.f;
-  int bw = b->tile_w, bh = b->tile_h, bs = b->stage;
+  int bw = b->tile_w, bh = b->tile_h, bs = b->stage, bu = b->steps;
   int rc = ALOHA_OK;
-  for (int k = 0; k < 8 && !rc; ++k) {
+  for (int k = 0; k < 12 && !rc; ++k) {
     const int* sh = shapes[k % 4];
-    const int stage = k / 4;  // ALOHA_STAGING_NONE, then ALOHA_STAGING_NEXT_SAMPLE
+    const int stage = forms[k / 4][0], steps = forms[k / 4][1];
     b->stage = stage;
+    b->steps = steps;
     rc = aloha_batch_set_config(b, sh[0], sh[1], 0);
     if (rc) break;
     rc = aloha_batch_launch(b, stream);  // warm-up
@@ -237,12 +260,14 @@ int aloha_batch_autotune(aloha_batch* b, void* stream, int reps, int* tile_w, in
       bw = sh[0];
       bh = sh[1];
       bs = stage;
+      bu = steps;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc) return rc;
   b->stage = bs;
+  b->steps = bu;
   rc = aloha_batch_set_config(b, bw, bh, 0);
   if (rc) return rc;
   *tile_w = bw;

@@ -159,7 +159,10 @@ cudaError_t launch_pad_brick(const float* src, int nx, int ny, int nz, float4* d
                              int* nonfinite_flag, cudaStream_t s);
 // Persistent render launch; `batch` selects the instance tuned for batches.
 constexpr int kSingleRenderBlocks = 5, kBatchRenderBlocks = 7;  // CTAs per SM
-// `stage`: ALOHA_STAGING_NONE or _NEXT_SAMPLE (the stencil loads).
+// `stage`: ALOHA_STAGING_NONE or _NEXT_SAMPLE (the stencil loads), or, for
+// batches, kStageUnroll2: direct loads with the march loop written out two
+// steps per trip.
+constexpr int kStageUnroll2 = 2;
 // `lane_groups`: the instance that renders the first a.group_chunks chunks of
 // the cost order with lane groups (single view, 8x4 chunks, direct loads).
 cudaError_t launch_render_warps(const BatchArgs& a, int chunk_w, int chunk_h, int grid, bool batch, cudaStream_t s,

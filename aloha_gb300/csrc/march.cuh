@@ -183,8 +183,16 @@ __device__ __forceinline__ StencilOut stencil(const float4* __restrict__ base, i
 // as the direct loads', so frames are bit-identical.
 struct DirectLoads {
   static constexpr bool kStaged = false;
+  static constexpr int kSteps = 1;  // march steps per loop trip
   __device__ __forceinline__ void begin_brick() {}
   __device__ __forceinline__ void finish() {}
+};
+
+// Direct loads with the march loop written out STEPS steps per trip (a
+// step-unrolled march: the same steps in the same order, the same bits).
+template <int STEPS>
+struct UnrolledDirectLoads : DirectLoads {
+  static constexpr int kSteps = STEPS;
 };
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -210,6 +218,7 @@ constexpr size_t kStageBytes = (size_t)2 * kStageRows * kRenderThreads * sizeof(
 
 struct StagedLoads {
   static constexpr bool kStaged = true;
+  static constexpr int kSteps = 1;
   float4* col;     // this thread's column: row e of slot k at col[(k * kStageRows + e) * kRenderThreads]
   float t_staged;  // t of the sample in slot `cur` (NaN: none)
   int cur;
@@ -365,6 +374,53 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
   // only has to be right for speed.
   float t_cell = t0;
   loads.begin_brick();
+  if constexpr (Loads::kSteps > 1 && !Hook::kActive && !Loads::kStaged) {
+    // The loop below for the render (no hook, direct loads), written out
+    // Loads::kSteps steps per trip.
+    auto step = [&]() -> bool {
+      if (!(t < t1 && color.w < et && n < cap)) return false;
+      const float ux = fmaf(t, r.d[0], r.o[0]) - lox;
+      const float uy = fmaf(t, r.d[1], r.o[1]) - loy;
+      const float uz = fmaf(t, r.d[2], r.o[2]) - loz;
+      if (empty && !(t < t_cell)) {
+        const int mx = min(max((int)floorf(ux), 0), nx - 1) >> kMacroShift;
+        const int my = min(max((int)floorf(uy), 0), ny - 1) >> kMacroShift;
+        const int mz = min(max((int)floorf(uz), 0), nz - 1) >> kMacroShift;
+        const float bx = (float)(mx << kMacroShift), by = (float)(my << kMacroShift),
+                    bz = (float)(mz << kMacroShift);
+        const float ex = ((r.d[0] > 0.f ? bx + (float)kMacro - eps : bx + eps) - offx) * idx_;
+        const float ey = ((r.d[1] > 0.f ? by + (float)kMacro - eps : by + eps) - offy) * idy;
+        const float ez = ((r.d[2] > 0.f ? bz + (float)kMacro - eps : bz + eps) - offz) * idz;
+        const float tb = fminf(fminf(fminf(ex, ey), ez), t1);
+        if (__ldg(empty + (mz * mny + my) * mnx + mx)) {
+          ++n;
+          t = t + dt;
+          if (exact) {
+            run_steps(t, n, tb, cap, dt, inv_dt, 0xffffffffu);
+          } else {
+            while (t < tb && n < cap) {
+              ++n;
+              t = t + dt;
+            }
+          }
+          return true;
+        }
+        t_cell = tb;
+      }
+      ++n;
+      const StencilOut s = stencil(base, sy, sz, nx, ny, nz, ux, uy, uz);
+      const float shade = shade_factor(s, r);
+      const float4 c = tf_lookup(tf_s, n_tf, nf, s.value);
+      composite_step(color, c, shade);
+      t = t + dt;
+      return true;
+    };
+    for (bool go = true; go;) {
+#pragma unroll
+      for (int k = 0; k < Loads::kSteps; ++k) go = go && step();
+    }
+    return n;
+  }
   while (t < t1 && color.w < et && n < cap) {
     const float ux = fmaf(t, r.d[0], r.o[0]) - lox;
     const float uy = fmaf(t, r.d[1], r.o[1]) - loy;

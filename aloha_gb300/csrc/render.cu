@@ -24,7 +24,8 @@ namespace aloha {
 // resident warps (7 CTAs, 72 registers).
 // STAGE selects the stencil loads: 0 direct, 1 the next sample's rows staged
 // in shared memory with cp.async (StagedLoads; shared memory after the
-// transfer function).  LG > 1 (single view in cost order, 8x4 chunks, frame
+// transfer function), kStageUnroll2 (batches) direct with the march loop
+// written out two steps per trip.  LG > 1 (single view in cost order, 8x4 chunks, frame
 // buffer only): work positions [0, LG * group_chunks) are the costliest
 // group_chunks chunks, each as LG items of 32 / LG pixels rendered by lane
 // groups of LG lanes per ray; the remaining positions are the other chunks of
@@ -34,7 +35,9 @@ __global__ void __launch_bounds__(kRenderThreads, MINB) render_warps_kernel(Batc
   extern __shared__ float4 tf_s[];
   load_tf(tf_s, b.f.tf, b.f.n_tf);
   __syncthreads();
-  using Loads = typename std::conditional<STAGE == 1, StagedLoads, DirectLoads>::type;
+  using Loads = typename std::conditional<
+      STAGE == 1, StagedLoads,
+      typename std::conditional<STAGE == kStageUnroll2, UnrolledDirectLoads<2>, DirectLoads>::type>::type;
   Loads loads;
   if constexpr (STAGE == 1) loads.init(tf_s + (b.f.n_tf + 4));
   const int lane = threadIdx.x & 31;
@@ -412,7 +415,9 @@ __global__ void macrocell_empty_kernel(const float2* __restrict__ ranges, int co
 }
 
 static size_t tf_smem(int n_tf) { return (size_t)(n_tf + 4) * sizeof(float4); }
-static size_t render_smem(int n_tf, int stage) { return tf_smem(n_tf) + (stage ? kStageBytes : 0); }
+static size_t render_smem(int n_tf, int stage) {
+  return tf_smem(n_tf) + (stage == ALOHA_STAGING_NEXT_SAMPLE ? kStageBytes : 0);
+}
 
 cudaError_t launch_macrocell_range(const DevBrick& b, float2* out, cudaStream_t s) {
   const int mnx = (b.n[0] + kMacro - 1) >> kMacroShift, mny = (b.n[1] + kMacro - 1) >> kMacroShift,
@@ -452,6 +457,8 @@ RenderKernel render_kernel(int chunk_w, int chunk_h, bool batch, int stage, bool
   if (stage == ALOHA_STAGING_NEXT_SAMPLE)
     return batch ? render_kernel_for<kBatchRenderBlocks, 1>(chunk_w, chunk_h)
                  : render_kernel_for<kSingleRenderBlocks, 1>(chunk_w, chunk_h);
+  if (stage == kStageUnroll2) return batch ? render_kernel_for<kBatchRenderBlocks, kStageUnroll2>(chunk_w, chunk_h)
+                                           : nullptr;
   if (stage != ALOHA_STAGING_NONE) return nullptr;
   return batch ? render_kernel_for<kBatchRenderBlocks, 0>(chunk_w, chunk_h)
                : render_kernel_for<kSingleRenderBlocks, 0>(chunk_w, chunk_h);

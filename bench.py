@@ -671,7 +671,7 @@ def batched_section(ctx, cams, mine, W, H, args, stream, dev, samples_of):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    stage = b.staging()
+    stage, steps = b.staging(), b.unroll()
     by_stage = staging_sweep(b, stream, timed)
     ms_graph = timed(lambda: b.launch_graph(stream))
 
@@ -682,8 +682,8 @@ def batched_section(ctx, cams, mine, W, H, args, stream, dev, samples_of):
     ms_plain = timed(plain)
     samples = sum(samples_of[ci] for ci in mine[:nv])
     b.close()
-    return {"views": nv, "tile": [tw, th], "staging": STAGING_NAMES[stage], "ms_batch_by_staging": by_stage,
-            "ms_batch": ms_graph, "ms_plain_launches": ms_plain,
+    return {"views": nv, "tile": [tw, th], "staging": STAGING_NAMES[stage], "unroll": steps,
+            "ms_batch_by_staging": by_stage, "ms_batch": ms_graph, "ms_plain_launches": ms_plain,
             "speedup_vs_plain": ms_plain / ms_graph, "gsamples_per_s": samples / (ms_graph * 1e-3) / 1e9}
 
 
@@ -691,14 +691,20 @@ STAGING_NAMES = {0: "none", 1: "next sample (cp.async, shared memory)"}
 
 
 def staging_sweep(b, stream, timed):
-    """Graph-launch time of the batch at its tuned tile with each staging
-    (untimed for the headline); leaves the tuned staging set."""
-    chosen = b.staging()
+    """Graph-launch time of the batch at its tuned tile with each staging, and
+    with direct loads two march steps per loop trip (untimed for the
+    headline); leaves the tuned staging and unroll set."""
+    chosen, steps = b.staging(), b.unroll()
     out = {}
+    b.set_unroll(1)
     for stage, name in STAGING_NAMES.items():
         b.set_staging(stage)
         out[name] = timed(lambda: b.launch_graph(stream))
+    b.set_staging(0)
+    b.set_unroll(2)
+    out["none, two steps per loop trip"] = timed(lambda: b.launch_graph(stream))
     b.set_staging(chosen)
+    b.set_unroll(steps)
     return out
 
 
@@ -760,7 +766,7 @@ def uneven_batched_section(vol, dev, big=64, small=32, staging=None, profile=Fal
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    stage = b.staging()
+    stage, steps = b.staging(), b.unroll()
     by_stage = staging_sweep(b, stream, timed)
     ms_batch = timed(lambda: b.launch_graph(stream))
     ms_plain = timed(lambda: [ctx.render(v, f, stream) for v, f in enumerate(fbs)])
@@ -768,7 +774,7 @@ def uneven_batched_section(vol, dev, big=64, small=32, staging=None, profile=Fal
     ctx.close()
     px = sum(w * w for w in sizes)
     return {"config": f"{n}^3 in {len(descs)} uneven bricks, {big} views at 1024^2 + {small} at 512^2",
-            "tile": [tw, th], "staging": STAGING_NAMES[stage], "ms_batch_by_staging": by_stage,
+            "tile": [tw, th], "staging": STAGING_NAMES[stage], "unroll": steps, "ms_batch_by_staging": by_stage,
             "ms_batch": ms_batch, "ms_plain_launches": ms_plain,
             "speedup_vs_plain": ms_plain / ms_batch, "gsamples_per_s": samples / (ms_batch * 1e-3) / 1e9,
             "ms_per_megapixel": ms_batch / (px / 2**20)}

@@ -259,11 +259,21 @@ int aloha_batch_get_config(const aloha_batch* b, int* tile_w, int* tile_h, int* 
  * aloha_set_render_staging). */
 int aloha_batch_set_staging(aloha_batch* b, int stage);
 int aloha_batch_get_staging(const aloha_batch* b, int* stage);
+
+/* March steps per loop trip of the batch's render kernel: 1 (default) or 2,
+ * the march loop written out two steps per trip (direct stencil loads only;
+ * with ALOHA_STAGING_NEXT_SAMPLE the setting is kept but not used).  Frames
+ * are bit-identical.  No reference counterpart (the step-unroll axis of the
+ * batch autotuner, which sweeps it with the chunk shape and the staging). */
+int aloha_batch_set_unroll(aloha_batch* batch, int steps);
+int aloha_batch_get_unroll(const aloha_batch* batch, int* steps);
+
 int aloha_batch_launch(aloha_batch* b, void* stream);
 int aloha_batch_launch_graph(aloha_batch* b, void* stream);
-/* Time every tile shape with each staging (`reps` launches each, CUDA
- * events) and keep the fastest; returns its shape and mean milliseconds per
- * launch (aloha_batch_get_staging gives its staging). */
+/* Time every tile shape with direct loads, direct loads two steps per trip,
+ * and staged loads (`reps` launches each, CUDA events) and keep the fastest;
+ * returns its shape and mean milliseconds per launch
+ * (aloha_batch_get_staging and aloha_batch_get_unroll give the rest). */
 int aloha_batch_autotune(aloha_batch* b, void* stream, int reps, int* tile_w, int* tile_h, float* ms);
 int aloha_batch_destroy(aloha_batch* b);
 

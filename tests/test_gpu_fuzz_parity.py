@@ -212,6 +212,7 @@ def test_random_batch_bit_exact(gpu_ctx_factory, oracle, seed):
     tile = [(8, 4), (8, 8), (16, 8), (32, 4)][int(rng.integers(0, 4))]
     b.set_config(*tile, int(rng.choice([0, 3, 5, 7])))
     b.set_staging(int(rng.choice([abi.STAGING_NONE, abi.STAGING_NEXT_SAMPLE])))
+    b.set_unroll(int(rng.choice([1, 2])))
     if rng.random() < 0.5:
         b.launch()
     else:

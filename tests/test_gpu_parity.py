@@ -211,8 +211,22 @@ def test_staged_batch_equals_direct_batch(gpu_ctx_factory):
         torch.cuda.synchronize()
         for f, s in zip(fbs, singles):
             assert_same_fb(f.cpu().numpy().view(np.uint32), s)
+    # direct loads with the march loop written out two steps per trip
+    b.set_staging(abi.STAGING_NONE)
+    for cfg in [(8, 4), (8, 8), (16, 8), (32, 4)]:
+        b.set_unroll(2)
+        b.set_config(*cfg)
+        assert b.unroll() == 2
+        for f in fbs:
+            f.zero_()
+        b.launch_graph() if cfg[0] == 8 else b.launch()
+        torch.cuda.synchronize()
+        for f, s in zip(fbs, singles):
+            assert_same_fb(f.cpu().numpy().view(np.uint32), s)
+    with pytest.raises(abi.AlohaError):
+        b.set_unroll(3)
     w, h, ms = b.autotune(reps=1)
-    assert b.staging() in (abi.STAGING_NONE, abi.STAGING_NEXT_SAMPLE) and ms > 0
+    assert b.staging() in (abi.STAGING_NONE, abi.STAGING_NEXT_SAMPLE) and b.unroll() in (1, 2) and ms > 0
     b.close()
 
 

@@ -54,10 +54,12 @@ class _FakeBatch:
         self.sweeps = 0
         self.config = None
         self.stage = 0
+        self.steps = 1
 
     def autotune(self, stream=None, reps=2):
         self.sweeps += 1
-        self.stage = 1
+        self.stage = 0
+        self.steps = 2
         return 32, 4, 1.5
 
     def set_config(self, w, h, c):
@@ -69,6 +71,12 @@ class _FakeBatch:
     def staging(self):
         return self.stage
 
+    def set_unroll(self, steps):
+        self.steps = steps
+
+    def unroll(self):
+        return self.steps
+
 
 def test_autotune_cache(tmp_path):
     path = str(tmp_path / "tune.json")
@@ -79,6 +87,7 @@ def test_autotune_cache(tmp_path):
     assert first["cached"] is False and b.sweeps == 1
     b2 = _FakeBatch()
     second = autotune.tune(b2, key, path=path)
-    assert second["cached"] is True and b2.sweeps == 0 and b2.config == (32, 4) and b2.stage == 1
+    assert second["cached"] is True and b2.sweeps == 0 and b2.config == (32, 4)
+    assert b2.stage == 0 and b2.steps == 2
     assert json.load(open(path))[key]["tile_w"] == 32
-    assert json.load(open(path))[key]["staging"] == 1
+    assert json.load(open(path))[key]["staging"] == 0 and json.load(open(path))[key]["unroll"] == 2
