@@ -78,3 +78,46 @@ def test_raw_volume_through_chopsuey_and_cpp_renderer(render_vol, oracle, tmp_pa
         np.testing.assert_array_equal(ctx.render(0, width=W, height=H), fb)
     ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H, oracle.make_params(), n_ranks=len(descs))
     np.testing.assert_array_equal(fb, ref["fb"])
+
+
+def test_cpp_training_views_match_oracle(oracle, tmp_path):
+    """tests/cpp/train_views.cpp: one aloha_forward_views launch over three
+    views and one aloha_backward_views call, from C++ with host buffers; the
+    images equal the oracle's and the gradients its FP64 adjoint's sum."""
+    from aloha_gb300 import abi
+    abi.lib()
+    exe = str(tmp_path / "train_views")
+    cxx = shutil.which("g++") or "g++"
+    lib_dir = os.path.join(ROOT, "aloha_gb300")
+    subprocess.run([cxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "train_views.cpp"), "-o", exe, "-L", lib_dir, "-laloha_gb300",
+                    f"-Wl,-rpath,{lib_dir}"], check=True)
+    n = 40
+    vol, descs, vox, tf = T.chopsuey_scene(n, 4)
+    W, H, k, nv = 48, 40, 16, 3
+    cams = T.cameras((n, n, n), nv, W, H, seed=47)
+    rng = np.random.default_rng(5)
+    dl = rng.uniform(-1, 1, (nv, H, W, 4)).astype(np.float32)
+    paths = {f: str(tmp_path / f) for f in ("s.vol", "tf.f32", "cams.f32", "dl.f32", "img.f32", "dtf.f32",
+                                             "dden.f32")}
+    V.write_vol(paths["s.vol"], (n, n, n), descs, vox)
+    tf.astype(np.float32).tofile(paths["tf.f32"])
+    np.asarray([[x for c in cam for x in c] for cam in cams], np.float32).tofile(paths["cams.f32"])
+    dl.tofile(paths["dl.f32"])
+    subprocess.run([exe, paths["s.vol"], paths["tf.f32"], str(tf.shape[0]), str(k), str(W), str(H), str(nv),
+                    paths["cams.f32"], paths["dl.f32"], paths["img.f32"], paths["dtf.f32"], paths["dden.f32"],
+                    str(n), str(n), str(n)], check=True)
+    img = np.fromfile(paths["img.f32"], np.float32).reshape(nv, H, W, 4)
+    dtf = np.fromfile(paths["dtf.f32"], np.float32).reshape(tf.shape[0], 4)
+    dden = np.fromfile(paths["dden.f32"], np.float32).reshape(n, n, n)
+    ref_tf = np.zeros((tf.shape[0], 4))
+    ref_den = np.zeros((n, n, n))
+    for v, cam in enumerate(cams):
+        ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H, oracle.make_params(), n_ranks=1,
+                            want=("final",))
+        np.testing.assert_array_equal(img[v], ref["final"])
+        r = oracle.adjoint(descs, vox, tf, oracle.make_camera(*cam), W, H, dl[v], (0, 0, 0), (n, n, n))
+        ref_tf += r["dtf"]
+        ref_den += r["ddensity"]
+    for got, want in ((dtf, ref_tf), (dden, ref_den)):
+        assert np.linalg.norm(got - want) / np.linalg.norm(want) < 2e-3
