@@ -9,6 +9,7 @@ import pytest
 
 from aloha_gb300 import abi
 from aloha_gb300 import scenes as S
+from aloha_gb300 import volfile as V
 from tests import scenes_for_tests as T
 
 pytestmark = pytest.mark.gpu
@@ -704,3 +705,38 @@ def test_two_contexts_are_independent(gpu_ctx_factory, oracle):
         np.testing.assert_array_equal(imgs[v].cpu().numpy(), ra["final"])
         rb = oracle.render(db, vb, tfb, oracle.make_camera(*cams_b[v]), W, H, oracle.make_params(**pb), n_ranks=3)
         assert_same_fb(fb[v].cpu().numpy().view(np.uint32), rb["fb"])
+
+
+@pytest.mark.parametrize("case", [
+    dict(dims=(40, 36, 44), dt=0.05),                      # many samples per ray
+    dict(dims=(40, 36, 44), dt=8.0),                       # steps longer than a macrocell
+    dict(dims=(40, 36, 44), et_alpha=0.01),                # rays end after almost nothing
+    dict(dims=(40, 36, 44), n_tf=1),                       # one transfer-function entry
+    dict(dims=(40, 36, 44), n_tf=2048),                    # the largest transfer function
+    dict(dims=(64, 64, 1)),                                # one voxel thick
+    dict(dims=(3, 50, 2)),                                 # thinner than the apron
+    dict(dims=(2, 2, 2)),                                  # two voxels a side
+    dict(dims=(40, 36, 44), size=(1, 1)),                  # a single pixel
+    dict(dims=(40, 36, 44), size=(1000, 3)),               # a wide strip
+])
+def test_edge_cases_bit_exact(gpu_ctx_factory, oracle, case):
+    """Extremes of the step, early termination, transfer-function size, volume
+    and frame shapes: the frame and sample count still equal the oracle's."""
+    dims = case["dims"]
+    rng = np.random.default_rng(sum(dims))
+    vol = S.blob_field(dims, 6, (1.0, 6.0), seed=int(rng.integers(1 << 20)))
+    vol = (vol * np.float32(1.2)).astype(np.float32)
+    descs = V.chopsuey_split(dims, 2)
+    vox = S.extract_bricks(vol, descs)
+    n_tf = case.get("n_tf", 256)
+    tf = S.seeded_tf(int(rng.integers(1 << 20)), n=max(n_tf, 2))[:n_tf].copy() if n_tf > 1 else \
+        np.array([[0.8, 0.4, 0.2, 0.3]], np.float32)
+    params = {k: case[k] for k in ("dt", "et_alpha") if k in case}
+    W, H = case.get("size", (64, 48))
+    ctx = setup_ctx(gpu_ctx_factory, descs, vox, tf, n_ranks=2, **params)
+    for seed in (1, 2):
+        cam = S.orbit_cameras(dims, 1, W, H, seed=seed, distance=1.5)[0]
+        fb, samples = gpu_frame(ctx, cam, W, H)
+        ref = oracle_frame(oracle, descs, vox, tf, cam, W, H, n_ranks=2, **params)
+        assert_same_fb(fb, ref["fb"])
+        assert samples == ref["samples"], (case, seed)
