@@ -486,12 +486,21 @@ inline void stencil_backward(const BrickView& b, const R u[3], R dv, const R dg[
   scatter_trilinear(b, u[0], u[1], u[2] - h, -dg[2], grid, gr);
 }
 
-// Transfer-function lookup backward: dch = dL/d(r,g,b,alpha) of the lookup.
-template <class R> inline R tf_backward(const float* tf, int n, R v, const R dch[4], R* dtf) {
-  R xb = v * R(n) - R(0.5);
-  R fl = std::floor(xb);
-  R w = xb - fl;
-  int i = to_int(fl);
+// The lookup and its backward on a given segment i (entries i, i+1) and the
+// shading with a given sign of N.d: the branch the float32 forward took at a
+// sample, evaluated in R (w may then leave [0, 1] by a rounding, the
+// continuous extension of that branch).
+template <class R> inline void tf_lookup_at(const float* tf, int n, R v, int i, R out[4]) {
+  const R w = v * R(n) - R(0.5) - R(i);
+  for (int ch = 0; ch < 4; ++ch) {
+    R e0 = (i >= 0 && i < n) ? R(tf[(size_t)i * 4 + ch]) : R(0);
+    R e1 = (i + 1 >= 0 && i + 1 < n) ? R(tf[(size_t)(i + 1) * 4 + ch]) : R(0);
+    out[ch] = lerp(e0, e1, w);
+  }
+}
+
+template <class R> inline R tf_backward_at(const float* tf, int n, R v, int i, const R dch[4], R* dtf) {
+  const R w = v * R(n) - R(0.5) - R(i);
   R dv = 0;
   for (int ch = 0; ch < 4; ++ch) {
     R e0 = (i >= 0 && i < n) ? R(tf[(size_t)i * 4 + ch]) : R(0);
@@ -513,14 +522,18 @@ template <class R> inline R tf_backward(const float* tf, int n, R v, const R dch
   return dv;
 }
 
-// Shading backward: s = .1 + .9 |q|, q = (g.d)/|g + 1e-4|.
-template <class R> inline void shade_backward(const R g[3], const R dir[3], R ds, R dg[3]) {
+template <class R> inline R shade_factor_signed(const R g[3], const R dir[3], int sgn) {
+  R e0 = g[0] + R(1e-4f), e1 = g[1] + R(1e-4f), e2 = g[2] + R(1e-4f);
+  R len = std::sqrt(std::fma(e2, e2, std::fma(e1, e1, e0 * e0)));
+  R gd = std::fma(g[2], dir[2], std::fma(g[1], dir[1], g[0] * dir[0]));
+  return std::fma(R(0.9f), R(sgn) * (gd / len), R(0.1f));
+}
+
+template <class R> inline void shade_backward_signed(const R g[3], const R dir[3], R ds, int sgn, R dg[3]) {
   R e[3] = {g[0] + R(1e-4f), g[1] + R(1e-4f), g[2] + R(1e-4f)};
   R len = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
   R gd = g[0] * dir[0] + g[1] * dir[1] + g[2] * dir[2];
-  R q = gd / len;
-  R sgn = q > 0 ? R(1) : (q < 0 ? R(-1) : R(0));
-  R k = ds * R(0.9f) * sgn;
+  R k = ds * R(0.9f) * R(sgn);
   for (int a = 0; a < 3; ++a) dg[a] = k * (dir[a] / len - gd * e[a] / (len * len * len));
 }
 
@@ -528,6 +541,8 @@ struct SampleRec {
   int brick;
   double t;
   double a;  // alpha before the sample
+  int seg;   // the float32 forward's transfer-function segment
+  int sgn;   // and its sign of N.d (shading)
 };
 
 // Adjoint of one pixel; returns the number of samples.
@@ -536,41 +551,71 @@ inline uint64_t adjoint_pixel(const BrickView* bricks, const float* tf, int n_tf
                               const Camera& cam, int W, int x, int y, const Params& p, const R dl[4], R* dtf,
                               R* dgrid, const Grid& gr) {
   const int pixel = x + W * y;
-  const R dt = R(p.dt), et = R(p.et_alpha);
+  // The sample set is the float32 forward's, the rendered image's: which
+  // samples are taken, at which t, and where the ray terminates (the walk of
+  // render_pixel for one rank); so are the branches of each sample's
+  // piecewise pieces, the transfer-function segment and the sign of N.d in
+  // the shading.  An R = double forward would decide some of these
+  // differently (a sample at a brick exit where the step is not exact in
+  // float, the sample that crosses the termination threshold, a value within
+  // a rounding of a transfer-function knot, N.d within a rounding of 0), and
+  // then differentiate another function than the image's.
+  std::vector<SampleRec> recs;
+  {
+    const float dt = p.dt, et = p.et_alpha;
+    float org[3], dir[3];
+    generate_ray(cam, x, y, org, dir);
+    float color[4] = {0.f, 0.f, 0.f, 0.f};
+    float tmin = 0.f;
+    uint32_t draw = 0;
+    const int r = sch.rank_order[0];
+    for (int j = sch.rank_start[r]; j < sch.rank_start[r + 1]; ++j) {
+      const int bi = sch.rank_bricks[j];
+      const BrickView& b = bricks[bi];
+      float t0, t1;
+      if (!slab(org, dir, b.space_lo, b.space_hi, tmin, 1e10f, t0, t1)) continue;
+      const float ils = jitter_value(p, (uint32_t)pixel, draw++);
+      const float span = (t1 - t0) / dt;
+      const uint64_t cap = span < 1e8f ? (uint64_t)(uint32_t)(span * 2.0f) + 16u : 200000016u;
+      uint64_t n = 0;
+      for (float t = first_sample_t(t0, dt, ils); t < t1 && color[3] < et && n < cap; t = t + dt) {
+        ++n;
+        float u[3];
+        for (int a = 0; a < 3; ++a) u[a] = std::fma(t, dir[a], org[a]) - b.lo[a];
+        Stencil<float> s = stencil(b, u);
+        const float shade = shade_factor(s.grad, dir);
+        float c[4];
+        tf_lookup(tf, n_tf, s.value, c);
+        const int seg = to_int(std::floor(s.value * (float)n_tf - 0.5f));
+        const float gd = std::fma(s.grad[2], dir[2], std::fma(s.grad[1], dir[1], s.grad[0] * dir[0]));
+        recs.push_back(SampleRec{bi, (double)t, 0.0, seg, gd > 0.f ? 1 : (gd < 0.f ? -1 : 0)});
+        const float oma = 1.0f - color[3];
+        const float s1 = oma * c[3];
+        color[0] = std::fma(s1 * c[0], shade, color[0]);
+        color[1] = std::fma(s1 * c[1], shade, color[1]);
+        color[2] = std::fma(s1 * c[2], shade, color[2]);
+        color[3] = std::fma(oma, c[3], color[3]);
+      }
+      tmin = t1 + 1e-20f;
+      if (!(color[3] < et)) break;
+    }
+  }
+  // the alpha before each sample, composited in R along that set
   R org[3], dir[3];
   generate_ray(cam, x, y, org, dir);
-  std::vector<SampleRec> recs;
-  R color[4] = {0, 0, 0, 0};
-  R tmin = R(0);
-  uint32_t draw = 0;
-  const int r = sch.rank_order[0];
-  for (int j = sch.rank_start[r]; j < sch.rank_start[r + 1]; ++j) {
-    const int bi = sch.rank_bricks[j];
-    const BrickView& b = bricks[bi];
-    R t0, t1;
-    if (!slab(org, dir, b.space_lo, b.space_hi, tmin, R(1e10f), t0, t1)) continue;
-    R ils = R(jitter_value(p, (uint32_t)pixel, draw++));
-    const float span = (float)(t1 - t0) / (float)dt;
-    const uint64_t cap = span < 1e8f ? (uint64_t)(uint32_t)(span * 2.0f) + 16u : 200000016u;
-    uint64_t n = 0;
-    for (R t = first_sample_t(t0, dt, ils); t < t1 && color[3] < et && n < cap; t = t + dt) {
-      ++n;
+  {
+    R alpha = R(0);
+    for (SampleRec& rec : recs) {
+      const BrickView& b = bricks[rec.brick];
+      const R t = R(rec.t);
       R u[3];
-      for (int a = 0; a < 3; ++a) u[a] = std::fma(t, dir[a], org[a]) - R(b.lo[a]);
+      for (int ax = 0; ax < 3; ++ax) u[ax] = std::fma(t, dir[ax], org[ax]) - R(b.lo[ax]);
       Stencil<R> s = stencil(b, u);
-      R shade = shade_factor(s.grad, dir);
       R c[4];
-      tf_lookup(tf, n_tf, s.value, c);
-      recs.push_back(SampleRec{bi, (double)t, (double)color[3]});
-      R oma = R(1) - color[3];
-      R s1 = oma * c[3];
-      color[0] = std::fma(s1 * c[0], shade, color[0]);
-      color[1] = std::fma(s1 * c[1], shade, color[1]);
-      color[2] = std::fma(s1 * c[2], shade, color[2]);
-      color[3] = std::fma(oma, c[3], color[3]);
+      tf_lookup_at(tf, n_tf, s.value, rec.seg, c);
+      rec.a = (double)alpha;
+      alpha = std::fma(R(1) - alpha, c[3], alpha);
     }
-    tmin = t1 + R(1e-20f);
-    if (!(color[3] < et)) break;
   }
   R gA = dl[3];
   for (size_t k = recs.size(); k-- > 0;) {
@@ -579,9 +624,9 @@ inline uint64_t adjoint_pixel(const BrickView* bricks, const float* tf, int n_tf
     R u[3];
     for (int ax = 0; ax < 3; ++ax) u[ax] = std::fma(t, dir[ax], org[ax]) - R(b.lo[ax]);
     Stencil<R> s = stencil(b, u);
-    R shade = shade_factor(s.grad, dir);
+    R shade = shade_factor_signed(s.grad, dir, recs[k].sgn);
     R c[4];
-    tf_lookup(tf, n_tf, s.value, c);
+    tf_lookup_at(tf, n_tf, s.value, recs[k].seg, c);
     const R oma = R(1) - a;
     const R gc = dl[0] * c[0] + dl[1] * c[1] + dl[2] * c[2];
     R dch[4];
@@ -589,9 +634,9 @@ inline uint64_t adjoint_pixel(const BrickView* bricks, const float* tf, int n_tf
     dch[3] = oma * (shade * gc + gA);
     const R ds = oma * c[3] * gc;
     gA = gA * (R(1) - c[3]) - c[3] * shade * gc;
-    const R dv = tf_backward(tf, n_tf, s.value, dch, dtf);
+    const R dv = tf_backward_at(tf, n_tf, s.value, recs[k].seg, dch, dtf);
     R dg[3];
-    shade_backward(s.grad, dir, ds, dg);
+    shade_backward_signed(s.grad, dir, ds, recs[k].sgn, dg);
     stencil_backward(b, u, dv, dg, dgrid, gr);
   }
   return recs.size();

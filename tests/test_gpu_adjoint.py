@@ -74,8 +74,8 @@ def test_backward_matches_fp64_oracle(gpu_ctx_factory, oracle, bricks, k):
         r = oracle.adjoint(descs, vox, tf, oracle.make_camera(*cam), W, H, dl, (0, 0, 0), (n, n, n))
         ref_tf += r["dtf"]
         ref_den += r["ddensity"]
-    assert rel_err(dtf, ref_tf) < 1e-3
-    assert rel_err(dden, ref_den) < 1e-3
+    assert rel_err(dtf, ref_tf) < 5e-4
+    assert rel_err(dden, ref_den) < 5e-4
     assert np.count_nonzero(dden) > 1000
 
 
@@ -103,7 +103,7 @@ def test_density_only_backward(gpu_ctx_factory, oracle, bricks):
         ctx.backward(v, dl, None, only_den, (0, 0, 0), (n, n, n))
         ref_den += oracle.adjoint(descs, vox, tf, oracle.make_camera(*cam), W, H, dl, (0, 0, 0), (n, n, n))["ddensity"]
     assert np.count_nonzero(only_den) > 1000
-    assert rel_err(only_den, ref_den) < 1e-3
+    assert rel_err(only_den, ref_den) < 5e-4
     np.testing.assert_allclose(only_den, full_den, rtol=1e-4, atol=1e-6 * float(np.abs(full_den).max()))
 
 
@@ -141,9 +141,9 @@ def test_inexact_step_sequences(gpu_ctx_factory, oracle, kw):
         r = oracle.adjoint(descs, vox, tf, oracle.make_camera(*cam), W, H, dl, (0, 0, 0), (n, n, n), params)
         ref_tf += r["dtf"]
         ref_den += r["ddensity"]
-    assert rel_err(dtf, ref_tf) < 1e-3
-    assert rel_err(dden, ref_den) < 1e-3
-    assert rel_err(only_den, ref_den) < 1e-3
+    assert rel_err(dtf, ref_tf) < 5e-4
+    assert rel_err(dden, ref_den) < 5e-4
+    assert rel_err(only_den, ref_den) < 5e-4
     assert np.count_nonzero(dden) > 1000
 
 
@@ -295,7 +295,7 @@ def test_tf_only_backward(gpu_ctx_factory, oracle, bricks):
         ctx.backward(v, dl, only_tf, None, None, None)
         ref_tf += oracle.adjoint(descs, vox, tf, oracle.make_camera(*cam), W, H, dl, (0, 0, 0), (n, n, n))["dtf"]
     assert np.count_nonzero(only_tf) > 100
-    assert rel_err(only_tf, ref_tf) < 1e-3
+    assert rel_err(only_tf, ref_tf) < 5e-4
     np.testing.assert_allclose(only_tf, full_tf, rtol=1e-4, atol=1e-6 * float(np.abs(full_tf).max()))
     with pytest.raises(abi.AlohaError) as e:
         ctx.backward(0, dl, None, None, None, None)
@@ -345,11 +345,10 @@ def test_backward_views_is_the_sum(gpu_ctx_factory, oracle, where):
         many_tf, many_den = many_tf.cpu().numpy(), many_den.cpu().numpy()
     many_tf -= start_tf
     many_den -= start_den
-    # three views of eight bricks: the float32 sums of the single calls sit
-    # near 1e-3 of FP64 on this scene, and the summed call must sit with them
+    # both forms against the FP64 adjoint (three views of eight bricks)
     for got_tf, got_den in ((one_tf, one_den), (many_tf, many_den)):
-        assert rel_err(got_tf, ref_tf) < 2e-3
-        assert rel_err(got_den, ref_den) < 2e-3
+        assert rel_err(got_tf, ref_tf) < 5e-4
+        assert rel_err(got_den, ref_den) < 5e-4
     np.testing.assert_allclose(many_tf, one_tf, rtol=1e-4, atol=1e-5 * float(np.abs(one_tf).max()))
     np.testing.assert_allclose(many_den, one_den, rtol=1e-4, atol=1e-5 * float(np.abs(one_den).max()))
     # the transfer-function-only form, and the argument checks
@@ -411,8 +410,8 @@ def test_forward_views_equals_single_forwards(gpu_ctx_factory, oracle, bricks):
         dtf = np.zeros((tf.shape[0], 4), np.float32)
         dden = np.zeros((n, n, n), np.float32)
         ctx.backward_views(views, dls, dtf, dden, (0, 0, 0), (n, n, n))
-        assert rel_err(dtf, ref_tf) < 2e-3, mixed
-        assert rel_err(dden, ref_den) < 2e-3, mixed
+        assert rel_err(dtf, ref_tf) < 5e-4, mixed
+        assert rel_err(dden, ref_den) < 5e-4, mixed
     with pytest.raises(abi.AlohaError) as e:
         ctx.forward_views([0, 0], [imgs[1], imgs[1]], 16)
     assert e.value.code == abi.ERR_INVALID_ARGUMENT
@@ -458,3 +457,55 @@ def test_autograd_gradient_flags_and_uploads(gpu_ctx_factory):
     ((render_views(r, tf, den_d, [0, 1], (W, W)) - target) ** 2).sum().backward()
     torch.testing.assert_close(den_d.grad, den_a.grad, rtol=1e-4, atol=1e-6 * float(den_a.grad.abs().max()))
     r.close()
+
+
+@pytest.mark.parametrize("case", [
+    dict(dims=(36, 32, 40), dt=0.1, k=64),        # long segments of short steps
+    dict(dims=(36, 32, 40), dt=4.0, k=1),         # a checkpoint before every long step
+    dict(dims=(36, 32, 40), et_alpha=0.05),       # rays end early
+    dict(dims=(36, 32, 40), n_tf=1),              # one transfer-function entry
+    dict(dims=(36, 32, 40), n_tf=2048),           # the largest transfer function
+    dict(dims=(48, 48, 1)),                       # one voxel thick
+    dict(dims=(3, 40, 2)),                        # thinner than the apron
+])
+def test_training_edge_cases(gpu_ctx_factory, oracle, case):
+    """Extremes of the step, checkpoint interval, early termination,
+    transfer-function size and volume shape for the differentiable form: the
+    forward image equals the oracle's and both gradients are within 5e-4 of
+    the FP64 adjoint."""
+    from aloha_gb300 import volfile as V
+    dims = case["dims"]
+    rng = np.random.default_rng(sum(dims) + 7)
+    vol = (S.blob_field(dims, 6, (1.0, 6.0), seed=int(rng.integers(1 << 20))) * np.float32(1.2)).astype(np.float32)
+    descs = V.chopsuey_split(dims, 2)
+    vox = S.extract_bricks(vol, descs)
+    n_tf = case.get("n_tf", 256)
+    tf = S.seeded_tf(int(rng.integers(1 << 20)), n=max(n_tf, 2))[:n_tf].copy() if n_tf > 1 else \
+        np.array([[0.8, 0.4, 0.2, 0.3]], np.float32)
+    params = {k: case[k] for k in ("dt", "et_alpha") if k in case}
+    ctx = setup(gpu_ctx_factory, descs, vox, tf, **params)
+    op = oracle.make_params(**params)
+    W, H = 48, 40
+    cams = S.orbit_cameras(dims, 2, W, H, seed=9, distance=1.5)
+    nx, ny, nz = dims
+    for v, cam in enumerate(cams):
+        ctx.set_camera(v, *cam)
+        ctx.resize(v, W, H)
+    imgs = [np.zeros((H, W, 4), np.float32) for _ in cams]
+    ctx.forward_views([0, 1], imgs, case.get("k", 32))
+    dls = [rng.uniform(-1, 1, (H, W, 4)).astype(np.float32) for _ in cams]
+    dtf = np.zeros((n_tf, 4), np.float32)
+    dden = np.zeros((nz, ny, nx), np.float32)
+    ctx.backward_views([0, 1], dls, dtf, dden, (0, 0, 0), (nx, ny, nz))
+    ref_tf = np.zeros((n_tf, 4))
+    ref_den = np.zeros((nz, ny, nx))
+    for cam, img, dl in zip(cams, imgs, dls):
+        ref = oracle.render(descs, vox, tf, oracle.make_camera(*cam), W, H, op, n_ranks=1, want=("final",))
+        np.testing.assert_array_equal(img, ref["final"])
+        r = oracle.adjoint(descs, vox, tf, oracle.make_camera(*cam), W, H, dl, (0, 0, 0), (nx, ny, nz), op)
+        ref_tf += r["dtf"]
+        ref_den += r["ddensity"]
+    if np.linalg.norm(ref_tf) > 0:
+        assert rel_err(dtf, ref_tf) < 5e-4, case
+    if np.linalg.norm(ref_den) > 0:
+        assert rel_err(dden, ref_den) < 5e-4, case

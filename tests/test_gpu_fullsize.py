@@ -209,6 +209,7 @@ def test_differentiable_configuration_fp64(gpu_ctx_factory, oracle):
         r = oracle.adjoint(descs, vox, tf, oracle.make_camera(*cam), 256, 256, grad_np[v], (0, 0, 0), (128, 128, 128))
         ref_tf += r["dtf"]
         ref_den += r["ddensity"]
+    # the configured bound; measured: about 3e-4 for the density gradient
     assert _rel(dtf, ref_tf) < 1e-3
     assert _rel(dden, ref_den) < 1e-3
     assert np.count_nonzero(dden) > 10**5
@@ -330,5 +331,5 @@ def test_near_opaque_backward_matches_fp64(gpu_ctx_factory, oracle, tf_kind, et_
         ref_tf += r["dtf"]
         ref_den += r["ddensity"]
     assert opaque > 200  # the case under test: rays that become opaque
-    assert _rel(dtf, ref_tf) < 1e-3
-    assert _rel(dden, ref_den) < 1e-3
+    assert _rel(dtf, ref_tf) < 5e-4
+    assert _rel(dden, ref_den) < 5e-4

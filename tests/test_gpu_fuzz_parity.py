@@ -20,7 +20,7 @@ Two more sweeps draw the batched launch (1 to 10 views of random sizes, every
 chunk shape, CTA count and staging, plain or graph launch; each view's frame
 bit-identical to the oracle's) and the differentiable form (random
 single-rank scenes and checkpoint intervals; the training forward's float
-image bit-identical, both gradients within 1e-3 of the FP64 adjoint), the
+image bit-identical, both gradients within 5e-4 of the FP64 adjoint), the
 multi-view training calls (one forward launch over many views, a summed
 backward), and one context driven through random call sequences.
 """
@@ -232,7 +232,7 @@ def test_random_batch_bit_exact(gpu_ctx_factory, oracle, seed):
 def test_random_differentiable_case(gpu_ctx_factory, oracle, seed):
     """The differentiable form on random single-rank scenes: the training
     forward's float image is bit-identical to the oracle's, and the gradients
-    of a random dL/dRGBA are within 1e-3 (relative 2-norm) of the FP64
+    of a random dL/dRGBA are within 5e-4 (relative 2-norm) of the FP64
     adjoint, for a random checkpoint interval."""
     rng = np.random.default_rng(9000 + seed)
     dims = tuple(int(x) for x in rng.integers(9, 49, size=3))
@@ -269,9 +269,9 @@ def test_random_differentiable_case(gpu_ctx_factory, oracle, seed):
         return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
     where = f"seed {seed}: dims {dims}, {len(descs)} bricks, {W}x{H}, K {k}, {params}, n_tf {tf.shape[0]}"
     if np.linalg.norm(r["dtf"]) > 0:
-        assert rel(dtf, r["dtf"]) < 1e-3, where
+        assert rel(dtf, r["dtf"]) < 5e-4, where
     if np.linalg.norm(r["ddensity"]) > 0:
-        assert rel(dden, r["ddensity"]) < 1e-3, where
+        assert rel(dden, r["ddensity"]) < 5e-4, where
 
 
 @pytest.mark.parametrize("seed", range(12))
@@ -381,7 +381,7 @@ def test_random_multi_view_training(gpu_ctx_factory, oracle, seed):
     """aloha_forward_views over 2 to 12 views of random sizes (1 to 96 pixels a
     side) in one launch: every image bit-identical to the oracle's; then
     aloha_backward_views over them, some re-forwarded at a second checkpoint
-    interval, with a random choice of gradients: the sums within 2e-3 of the
+    interval, with a random choice of gradients: the sums within 5e-4 of the
     FP64 adjoints' sum."""
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(11000 + seed)
@@ -439,6 +439,6 @@ def test_random_multi_view_training(gpu_ctx_factory, oracle, seed):
         return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
     where = f"seed {seed}: {n_views} views, k {k}, re-forwarded {again}, gradients tf {want_tf} density {want_den}"
     if want_tf and np.linalg.norm(ref_tf) > 0:
-        assert rel(dtf, ref_tf) < 2e-3, where
+        assert rel(dtf, ref_tf) < 5e-4, where
     if want_den and np.linalg.norm(ref_den) > 0:
-        assert rel(dden, ref_den) < 2e-3, where
+        assert rel(dden, ref_den) < 5e-4, where
