@@ -185,6 +185,27 @@ float ora_first_sample_t(float lower, float dt, float ils) { return first_sample
 
 void ora_tf_lookup(const float* tf, int n, float v, float* out) { tf_lookup<float>(tf, n, v, out); }
 
+// The ordered composite of n float rank images ([n][npx][4]) front to back
+// in `order`, fp32 or RGBA8 blend, into RGBA8 pixels.
+void ora_composite_over(const float* images, const int* order, int n, int npx, int mode, uint32_t* fb) {
+  for (int px = 0; px < npx; ++px) {
+    float comp[4] = {0.f, 0.f, 0.f, 0.f};
+    uint32_t comp8[4] = {0u, 0u, 0u, 0u};
+    for (int k = 0; k < n; ++k) blend_over(mode, images + ((size_t)order[k] * npx + px) * 4, comp, comp8);
+    fb[px] = mode == COMPOSITE_UBYTE ? (comp8[0] | (comp8[1] << 8) | (comp8[2] << 16) | (comp8[3] << 24))
+                                     : pack_rgba(comp);
+  }
+}
+
+// The same for RGBA8 rank images ([n][npx] packed RGBA8).
+void ora_composite_over_rgba8(const uint32_t* images, const int* order, int n, int npx, uint32_t* fb) {
+  for (int px = 0; px < npx; ++px) {
+    uint32_t comp8[4] = {0u, 0u, 0u, 0u};
+    for (int k = 0; k < n; ++k) blend_over_rgba8(images[(size_t)order[k] * npx + px], comp8);
+    fb[px] = comp8[0] | (comp8[1] << 8) | (comp8[2] << 16) | (comp8[3] << 24);
+  }
+}
+
 void ora_stencil(const float* voxels, const int* n, const float* u, float* out4) {
   BrickView b{};
   b.voxels = voxels;

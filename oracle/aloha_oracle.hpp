@@ -337,6 +337,28 @@ template <class R> struct Outputs {
   uint64_t* samples;     // total samples over the rows rendered
 };
 
+// The IceT ordered BLEND of one rank image under the composite so far
+// (waikikiRenderer.cpp:1042-1077): premultiplied "over" in fp32 (one fused
+// multiply-add per channel), or IceT's RGBA8 form (quantise the rank image,
+// blend in 8 bits with rounding).
+template <class R>
+inline void blend_over(int mode, const R img[4], R comp[4], uint32_t comp8[4]) {
+  if (mode == COMPOSITE_UBYTE) {
+    uint32_t q[4] = {quantize8(img[0]), quantize8(img[1]), quantize8(img[2]), quantize8(img[3])};
+    uint32_t f = 255u - comp8[3];
+    for (int ch = 0; ch < 4; ++ch) comp8[ch] = std::min(255u, comp8[ch] + (q[ch] * f + 127u) / 255u);
+  } else {
+    R oma = R(1) - comp[3];
+    for (int ch = 0; ch < 4; ++ch) comp[ch] = std::fma(oma, img[ch], comp[ch]);
+  }
+}
+
+// The same for an RGBA8 rank image (the blend of IceT's RGBA_UBYTE images).
+inline void blend_over_rgba8(uint32_t q, uint32_t comp8[4]) {
+  const uint32_t f = 255u - comp8[3];
+  for (int ch = 0; ch < 4; ++ch) comp8[ch] = std::min(255u, comp8[ch] + (((q >> (8 * ch)) & 255u) * f + 127u) / 255u);
+}
+
 // One pixel: every virtual rank marches its own bricks (with its own early
 // termination, as each MPI rank does in the reference), runs renderFrame's
 // output stage, and the rank images are blended front to back.
@@ -404,14 +426,7 @@ inline uint64_t render_pixel(const BrickView* bricks, const float* tf, int n_tf,
     if (out.rank_images)
       for (int ch = 0; ch < 4; ++ch) out.rank_images[((size_t)r * npx + pixel) * 4 + ch] = img[ch];
     if (out.rank_depth) out.rank_depth[(size_t)r * npx + pixel] = (float)z;
-    if (p.composite_mode == COMPOSITE_UBYTE) {
-      uint32_t q[4] = {quantize8(img[0]), quantize8(img[1]), quantize8(img[2]), quantize8(img[3])};
-      uint32_t f = 255u - comp8[3];
-      for (int ch = 0; ch < 4; ++ch) comp8[ch] = std::min(255u, comp8[ch] + (q[ch] * f + 127u) / 255u);
-    } else {
-      R oma = R(1) - comp[3];
-      for (int ch = 0; ch < 4; ++ch) comp[ch] = std::fma(oma, img[ch], comp[ch]);
-    }
+    blend_over(p.composite_mode, img, comp, comp8);
     total += ns;
   }
   if (out.final_rgba)

@@ -165,6 +165,35 @@ def partition_kd(descs, n_ranks: int):
     return cr, kd[:k].copy()
 
 
+def composite_over(images: np.ndarray, order, mode: int = COMPOSITE_FP32) -> np.ndarray:
+    """The ordered composite (IceT stand-in) of float rank images [n][H][W][4]
+    front to back in `order`: RGBA8 frame [H][W]."""
+    images = np.ascontiguousarray(images, dtype=np.float32)
+    n, H, W = images.shape[:3]
+    o = np.ascontiguousarray(order, dtype=np.int32)
+    fb = np.zeros((H, W), np.uint32)
+    L = lib()
+    L.ora_composite_over.argtypes = [c_float_p, c_int_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_uint32)]
+    L.ora_composite_over(_ptr(images, ctypes.c_float), _ptr(o, ctypes.c_int), o.size, H * W, int(mode),
+                         _ptr(fb, ctypes.c_uint32))
+    return fb
+
+
+def composite_over_rgba8(images: np.ndarray, order) -> np.ndarray:
+    """The same for RGBA8 rank images [n][H][W] (packed uint32)."""
+    images = np.ascontiguousarray(images, dtype=np.uint32)
+    n, H, W = images.shape
+    o = np.ascontiguousarray(order, dtype=np.int32)
+    fb = np.zeros((H, W), np.uint32)
+    L = lib()
+    L.ora_composite_over_rgba8.argtypes = [ctypes.POINTER(ctypes.c_uint32), c_int_p, ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_uint32)]
+    L.ora_composite_over_rgba8(_ptr(images, ctypes.c_uint32), _ptr(o, ctypes.c_int), o.size, H * W,
+                               _ptr(fb, ctypes.c_uint32))
+    return fb
+
+
 def composite_order_kd(kd: np.ndarray, ref, n_ranks: int) -> list[int]:
     r = np.asarray(ref, dtype=np.float32)
     kd = np.ascontiguousarray(kd, dtype=np.int32)

@@ -22,7 +22,8 @@ bit-identical to the oracle's) and the differentiable form (random
 single-rank scenes and checkpoint intervals; the training forward's float
 image bit-identical, both gradients within 5e-4 of the FP64 adjoint), the
 multi-view training calls (one forward launch over many views, a summed
-backward), and one context driven through random call sequences.
+backward), the standalone composites, and one context driven through random
+call sequences.
 """
 import numpy as np
 import pytest
@@ -442,3 +443,37 @@ def test_random_multi_view_training(gpu_ctx_factory, oracle, seed):
         assert rel(dtf, ref_tf) < 5e-4, where
     if want_den and np.linalg.norm(ref_den) > 0:
         assert rel(dden, ref_den) < 5e-4, where
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_random_standalone_composites(oracle, seed):
+    """The IceT stand-ins on their own: 1 to 64 random rank images (values
+    partly outside [0, 1], so the quantisation clamps), a random order, both
+    blend modes, through aloha_composite_over (device and host images),
+    aloha_composite_over_noalloc and, for RGBA8 rank images,
+    aloha_composite_over_rgba8; every frame equals the oracle's blend."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(13000 + seed)
+    n = int(rng.choice([1, 2, 5, 12, 33, 64]))
+    W, H = (int(x) for x in rng.choice([1, 7, 40, 96], size=2))
+    imgs = rng.uniform(-0.1, 1.1, (n, H, W, 4)).astype(np.float32)
+    imgs[..., :3] *= np.clip(imgs[..., 3:4], 0, 1)  # mostly premultiplied
+    order = rng.permutation(n).astype(np.int32)
+    L = abi.lib()
+    stream = torch.cuda.current_stream()
+    dev_imgs = torch.from_numpy(imgs).cuda()
+    for mode in (abi.COMPOSITE_FP32, abi.COMPOSITE_UBYTE):
+        want = oracle.composite_over(imgs, order, mode)
+        host_out = abi.composite_over(imgs, order, W, H, mode)
+        dev_out = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+        abi.composite_over(dev_imgs, order, W, H, mode, fb=dev_out, stream=stream)
+        na_out = torch.full((H, W), -1, dtype=torch.int32, device="cuda")
+        assert L.aloha_composite_over_noalloc(dev_imgs.data_ptr(), order.ctypes.data, n, W, H, mode,
+                                              na_out.data_ptr(), stream.cuda_stream) == abi.OK
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(host_out, want, err_msg=f"seed {seed} mode {mode} host")
+        np.testing.assert_array_equal(dev_out.cpu().numpy().view(np.uint32), want, err_msg=f"seed {seed} device")
+        np.testing.assert_array_equal(na_out.cpu().numpy().view(np.uint32), want, err_msg=f"seed {seed} noalloc")
+    packed = rng.integers(0, 2**32, (n, H, W), dtype=np.uint64).astype(np.uint32)
+    np.testing.assert_array_equal(abi.composite_over_rgba8(packed, order, W, H),
+                                  oracle.composite_over_rgba8(packed, order), err_msg=f"seed {seed} rgba8")
