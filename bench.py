@@ -503,6 +503,7 @@ def main():
             adj.append(adjoint_section("128^3 single brick, 16 x 256^2", v4, S.single_brick((128, 128, 128)), c4,
                                        256, 256, args.adjoint_k, stream, dev))
             result["adjoint"] = adj
+            result["autograd"] = autograd_section(dev)
 
         if not args.no_cpu_baseline and rank == 0:
             vol_np = vol.cpu().numpy()
@@ -645,6 +646,49 @@ def adjoint_section(name, vol, descs, cams, W, H, k, stream, dev):
             "samples_per_view": samples / nv,
             "fwd_gsamples_per_s": samples / (fwd_ms * 1e-3) / 1e9,
             "fwd_plus_adjoint_gsamples_per_s": samples / ((fwd_ms + bwd_ms) * 1e-3) / 1e9}
+
+
+def autograd_section(dev, steps=5):
+    """The differentiable configuration through the torch binding, the call a
+    training loop makes: render_views of 16 views (one forward launch), an L2
+    loss against targets of a second transfer function, loss.backward() for
+    the transfer-function and density gradients (one summed backward).  CUDA
+    events around whole steps."""
+    import torch
+
+    from aloha_gb300 import scenes as S
+    from aloha_gb300.autograd import DifferentiableRenderer, render_views
+    dims = (128, 128, 128)
+    den = S.blob_field(dims, 16, (4.0, 12.0), seed=4001, device=dev).contiguous().requires_grad_(True)
+    cams = S.orbit_cameras(dims, 16, 256, 256, seed=4002)
+    r = DifferentiableRenderer(dims, bricks=1, checkpoint_every=32)
+    for v, cam in enumerate(cams):
+        r.set_camera(v, cam, 256, 256)
+    views = list(range(16))
+    with torch.no_grad():
+        target = render_views(r, torch.from_numpy(S.seeded_tf(77)).to(dev), den.detach(), views, (256, 256))
+    tf = torch.from_numpy(S.ramp_tf()).to(dev).requires_grad_(True)
+
+    def step():
+        tf.grad = None
+        den.grad = None
+        loss = ((render_views(r, tf, den, views, (256, 256)) - target) ** 2).sum()
+        loss.backward()
+
+    for _ in range(3):
+        step()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    r.close()
+    return {"config": "128^3 single brick, 16 x 256^2, torch.autograd (render_views, L2 loss, both gradients)",
+            "ms_per_step": ms, "ms_per_view": ms / 16}
 
 
 def batched_section(ctx, cams, mine, W, H, args, stream, dev, samples_of):
