@@ -19,6 +19,13 @@
 // per CTA), the shading and the seven-tap stencil (20 voxel weights, atomic
 // adds into the density gradient on the caller's grid).  Early termination is
 // held fixed, as usual for a discontinuity.
+//
+// One launch serves one view or many: the forward marches the chunks of all
+// its views position-major (every view's first chunk, then every view's
+// second, ...), and the backward replays the segments of all its views, each
+// item finding its view in a prefix of the views' segment counts.  A launch
+// of one view passes it in the kernel parameters instead (backward_kernel's
+// MULTI = false), which keeps its pointers out of the replay's registers.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
