@@ -5,7 +5,9 @@
 table ``tf`` (n, 4) and the density volume ``density`` (nz, ny, nx), both CUDA
 float32 tensors.  The forward stores the march state every K samples; the
 backward replays each K-sample segment from its checkpoint in parallel (see
-csrc/adjoint.cu) and accumulates the gradients.
+csrc/adjoint.cu) and accumulates the gradients.  All views of one call go
+through one training-forward launch (aloha_forward_views) and one summed
+backward (aloha_backward_views).
 """
 from __future__ import annotations
 
