@@ -353,46 +353,73 @@ __global__ void composite_u8_kernel(const uint32_t* __restrict__ imgs, const int
 
 // Copies a brick (x fastest) into its padded x-quad array: element (x,y,z)
 // holds V(x..x+3) with every index clamped to the brick (the apron and the
-// quad tails repeat edge values), and flags non-finite voxels.
+// quad tails repeat edge values), and flags non-finite voxels.  CTAs take
+// padded rows (y, z), their threads the row's elements, so the index
+// arithmetic is one division per row.
 __global__ void pad_brick_kernel(const float* __restrict__ src, int nx, int ny, int nz, float4* __restrict__ dst,
                                  int px, int py, int pz, int* nonfinite) {
-  const size_t total = (size_t)px * py * pz;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-    const int x = (int)(i % px);
-    const int y = (int)((i / px) % py);
-    const int z = (int)(i / ((size_t)px * py));
+  const int rows = py * pz;
+  bool bad = false;
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int y = r % py, z = r / py;
     const int sy = min(max(y - kApron, 0), ny - 1);
     const int sz = min(max(z - kApron, 0), nz - 1);
-    const float* row = src + ((size_t)sz * ny + sy) * nx;
-    float v[4];
+    const float* __restrict__ row = src + ((size_t)sz * ny + sy) * nx;
+    float4* __restrict__ out = dst + (size_t)r * px;
+    for (int x = threadIdx.x; x < px; x += blockDim.x) {
+      float v[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) v[k] = row[min(max(x - kApron + k, 0), nx - 1)];
-    if (!isfinite(v[0]) || !isfinite(v[1]) || !isfinite(v[2]) || !isfinite(v[3])) atomicOr(nonfinite, 1);
-    dst[i] = make_float4(v[0], v[1], v[2], v[3]);
+      for (int k = 0; k < 4; ++k) v[k] = __ldg(row + min(max(x - kApron + k, 0), nx - 1));
+      bad |= !isfinite(v[0]) || !isfinite(v[1]) || !isfinite(v[2]) || !isfinite(v[3]);
+      out[x] = make_float4(v[0], v[1], v[2], v[3]);
+    }
   }
+  if (bad) atomicOr(nonfinite, 1);
 }
 
 // Value range each macrocell's samples can read: a sample whose value-tap
 // cell is c (c = clamp(floor(u), 0, n-1)) reads voxels c and c+1 (clamped), so
-// macrocell m covers voxels [m*kMacro, m*kMacro + kMacro] per axis.
+// macrocell m covers voxels [m*kMacro, m*kMacro + kMacro] per axis.  One warp
+// per macrocell: its lanes split the macrocell's (y, z) rows, read each row
+// as x-quads (four voxels per load, the components inside the range used),
+// and combine their minima and maxima with shuffles.
 __global__ void macrocell_range_kernel(const float4* __restrict__ base, int sy, int sz, int nx, int ny, int nz,
                                        int mnx, int mny, int mnz, float2* __restrict__ out) {
   const int total = mnx * mny * mnz;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < total; i += warps) {
     const int mx = i % mnx, my = (i / mnx) % mny, mz = i / (mnx * mny);
     const int x0 = mx * kMacro, y0 = my * kMacro, z0 = mz * kMacro;
     const int x1 = min(x0 + kMacro, nx - 1), y1 = min(y0 + kMacro, ny - 1), z1 = min(z0 + kMacro, nz - 1);
+    const int rows_y = y1 - y0 + 1, rows = rows_y * (z1 - z0 + 1);
     float lo = __int_as_float(0x7f800000), hi = -lo;
-    for (int z = z0; z <= z1; ++z)
-      for (int y = y0; y <= y1; ++y) {
-        const float4* row = base + (size_t)z * sz + (size_t)y * sy;
-        for (int x = x0; x <= x1; ++x) {
-          const float v = __ldg(row + x).x;
-          lo = fminf(lo, v);
-          hi = fmaxf(hi, v);
+    for (int r = lane; r < rows; r += 32) {
+      const float4* row = base + (size_t)(z0 + r / rows_y) * sz + (size_t)(y0 + r % rows_y) * sy;
+      for (int x = x0; x <= x1; x += 4) {
+        const float4 q = __ldg(row + x);
+        lo = fminf(lo, q.x);
+        hi = fmaxf(hi, q.x);
+        if (x + 1 <= x1) {
+          lo = fminf(lo, q.y);
+          hi = fmaxf(hi, q.y);
+        }
+        if (x + 2 <= x1) {
+          lo = fminf(lo, q.z);
+          hi = fmaxf(hi, q.z);
+        }
+        if (x + 3 <= x1) {
+          lo = fminf(lo, q.w);
+          hi = fmaxf(hi, q.w);
         }
       }
-    out[i] = make_float2(lo, hi);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, d));
+      hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, d));
+    }
+    if (lane == 0) out[i] = make_float2(lo, hi);
   }
 }
 
@@ -423,7 +450,7 @@ cudaError_t launch_macrocell_range(const DevBrick& b, float2* out, cudaStream_t 
   const int mnx = (b.n[0] + kMacro - 1) >> kMacroShift, mny = (b.n[1] + kMacro - 1) >> kMacroShift,
             mnz = (b.n[2] + kMacro - 1) >> kMacroShift;
   const int total = mnx * mny * mnz;
-  const int grid = total < 256 ? 1 : min((total + 127) / 128, 152 * 32);
+  const int grid = min((total + 3) / 4, 152 * 32);  // 4 warps (macrocells) per CTA
   macrocell_range_kernel<<<grid, 128, 0, s>>>(b.base, b.sy, b.sz, b.n[0], b.n[1], b.n[2], mnx, mny, mnz, out);
   return cudaGetLastError();
 }
@@ -539,11 +566,9 @@ cudaError_t launch_composite_u8(const uint32_t* imgs, const int* order, int n_ra
 
 cudaError_t launch_pad_brick(const float* src, int nx, int ny, int nz, float4* dst, int px, int py, int pz,
                              int* nonfinite, cudaStream_t s) {
-  const size_t total = (size_t)px * py * pz;
-  size_t g = (total + 255) / 256;
-  if (g > 152 * 64) g = 152 * 64;
-  if (g < 1) g = 1;
-  pad_brick_kernel<<<(unsigned)g, 256, 0, s>>>(src, nx, ny, nz, dst, px, py, pz, nonfinite);
+  const int rows = py * pz;
+  const int g = rows < 152 * 32 ? rows : 152 * 32;  // CTAs of 128 threads take rows
+  pad_brick_kernel<<<g < 1 ? 1 : g, 128, 0, s>>>(src, nx, ny, nz, dst, px, py, pz, nonfinite);
   return cudaGetLastError();
 }
 
