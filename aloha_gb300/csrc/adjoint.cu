@@ -367,14 +367,18 @@ __device__ __forceinline__ void stencil_backward(const DevBrick& b, const TrainA
     scatter2(a, b, org, cx, min(max(cy + j, 0), ny1), ze, wze * wx[0] * wy[j], wze * wx[1] * wy[j]);
 }
 
-// out[v] += q[v].x + q[v-1].y + q[v-2].z along x (each voxel written by one thread).
-__global__ void fold_quads_kernel(const float4* __restrict__ q, float* __restrict__ out, int dx, size_t total) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-    const int x = (int)(i % (size_t)dx);
-    float s = q[i].x;
-    if (x >= 1) s += q[i - 1].y;
-    if (x >= 2) s += q[i - 2].z;
-    if (s != 0.f) out[i] += s;
+// out[v] += q[v].x + q[v-1].y + q[v-2].z along x (each voxel written by one
+// thread).  CTAs take grid rows (y, z), their threads the row's voxels.
+__global__ void fold_quads_kernel(const float4* __restrict__ q, float* __restrict__ out, int dx, int rows) {
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+    const float4* __restrict__ qr = q + (size_t)r * dx;
+    float* __restrict__ orow = out + (size_t)r * dx;
+    for (int x = threadIdx.x; x < dx; x += blockDim.x) {
+      float s = qr[x].x;
+      if (x >= 1) s += qr[x - 1].y;
+      if (x >= 2) s += qr[x - 2].z;
+      if (s != 0.f) orow[x] += s;
+    }
   }
 }
 
@@ -692,11 +696,11 @@ cudaError_t launch_backward(const TrainArgs& a, int grid, cudaStream_t s) {
 }
 
 cudaError_t launch_fold_quads(const float4* quads, float* out, const int dims[3], cudaStream_t s) {
-  const size_t total = (size_t)dims[0] * dims[1] * dims[2];
-  size_t grid = (total + 255) / 256;
-  if (grid > 152 * 32) grid = 152 * 32;
-  if (grid < 1) grid = 1;
-  fold_quads_kernel<<<(unsigned)grid, 256, 0, s>>>(quads, out, dims[0], total);
+  const long long rows = (long long)dims[1] * dims[2];
+  if (rows <= 0 || rows > 0x7fffffffll) return cudaErrorInvalidValue;
+  const int threads = dims[0] >= 256 ? 256 : 128;
+  const int grid = (int)(rows < 152 * 32 ? rows : 152 * 32);
+  fold_quads_kernel<<<grid, threads, 0, s>>>(quads, out, dims[0], (int)rows);
   return cudaGetLastError();
 }
 
