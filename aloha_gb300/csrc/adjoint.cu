@@ -368,16 +368,35 @@ __device__ __forceinline__ void stencil_backward(const DevBrick& b, const TrainA
 }
 
 // out[v] += q[v].x + q[v-1].y + q[v-2].z along x (each voxel written by one
-// thread).  CTAs take grid rows (y, z), their threads the row's voxels.
-__global__ void fold_quads_kernel(const float4* __restrict__ q, float* __restrict__ out, int dx, int rows) {
+// thread), leaving every quad it read zero again: a quad is rewritten only if
+// it was nonzero, so a backward that touched part of the grid pays for that
+// part only, and the next backward finds the buffer clear without a memset.
+// CTAs take grid rows (y, z) and walk each in chunks of blockDim.x quads
+// staged in shared memory behind the previous chunk's last two, so no quad
+// is cleared before its three readers have it.
+__global__ void fold_quads_kernel(float4* __restrict__ q, float* __restrict__ out, int dx, int rows) {
+  extern __shared__ float4 sq[];  // [2 + blockDim.x]: q[x0-2], q[x0-1], then the chunk
+  const int bd = (int)blockDim.x, i = (int)threadIdx.x;
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int r = blockIdx.x; r < rows; r += gridDim.x) {
-    const float4* __restrict__ qr = q + (size_t)r * dx;
+    float4* __restrict__ qr = q + (size_t)r * dx;
     float* __restrict__ orow = out + (size_t)r * dx;
-    for (int x = threadIdx.x; x < dx; x += blockDim.x) {
-      float s = qr[x].x;
-      if (x >= 1) s += qr[x - 1].y;
-      if (x >= 2) s += qr[x - 2].z;
-      if (s != 0.f) orow[x] += s;
+    if (i < 2) sq[i] = zero;
+    for (int x0 = 0; x0 < dx; x0 += bd) {
+      const int x = x0 + i;
+      const float4 v = x < dx ? qr[x] : zero;
+      sq[2 + i] = v;
+      __syncthreads();
+      if (x < dx) {
+        float s = v.x;
+        if (x >= 1) s += sq[1 + i].y;
+        if (x >= 2) s += sq[i].z;
+        if (s != 0.f) orow[x] += s;
+        if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) qr[x] = zero;
+      }
+      __syncthreads();
+      if (i < 2) sq[i] = sq[bd + i];
+      __syncthreads();
     }
   }
 }
@@ -695,12 +714,12 @@ cudaError_t launch_backward(const TrainArgs& a, int grid, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_fold_quads(const float4* quads, float* out, const int dims[3], cudaStream_t s) {
+cudaError_t launch_fold_quads(float4* quads, float* out, const int dims[3], cudaStream_t s) {
   const long long rows = (long long)dims[1] * dims[2];
-  if (rows <= 0 || rows > 0x7fffffffll) return cudaErrorInvalidValue;
+  if (rows <= 0 || rows > 0x7fffffffll || dims[0] <= 0) return cudaErrorInvalidValue;
   const int threads = dims[0] >= 256 ? 256 : 128;
   const int grid = (int)(rows < 152 * 32 ? rows : 152 * 32);
-  fold_quads_kernel<<<grid, threads, 0, s>>>(quads, out, dims[0], (int)rows);
+  fold_quads_kernel<<<grid, threads, (threads + 2) * sizeof(float4), s>>>(quads, out, dims[0], (int)rows);
   return cudaGetLastError();
 }
 

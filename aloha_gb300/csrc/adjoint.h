@@ -82,8 +82,9 @@ cudaError_t launch_forward_train(const TrainArgs& a, unsigned items, int max_gri
 int forward_train_blocks_per_sm(int n_tf);
 // One persistent backward over the launch's views' items (a.tv, a.item_base).
 cudaError_t launch_backward(const TrainArgs& a, int grid, cudaStream_t s);
-// out[v] += quads[v].x + quads[v-1].y + quads[v-2].z along x, for a grid of dims.
-cudaError_t launch_fold_quads(const float4* quads, float* out, const int dims[3], cudaStream_t s);
+// out[v] += quads[v].x + quads[v-1].y + quads[v-2].z along x, for a grid of
+// dims; every quad of the grid is zero afterwards.
+cudaError_t launch_fold_quads(float4* quads, float* out, const int dims[3], cudaStream_t s);
 int backward_blocks_per_sm(int n_tf);
 
 }  // namespace aloha

@@ -138,6 +138,10 @@ struct aloha_ctx {
   aloha_render_params params;
   DeviceBuffer counter, flag, staging_out, work, grad4;
   DeviceBuffer train_tables;  // per launch of the differentiable form: item counter, views, runs
+  // every byte of grad4 is zero once the stream reaches the last fold (the
+  // fold clears the quads it reads); false after a reallocation or a backward
+  // that returned before its fold was enqueued
+  bool grad4_zero = false;
   // persistent render of one view: chunk shape and grid (occupancy depends on
   // the transfer-function size through shared memory)
   int chunk_w = 0, chunk_h = 0;  // 0 = automatic
@@ -1476,10 +1480,14 @@ int backward_views(aloha_ctx* c, int n_views, const int* view_ids, const float* 
   float* grid_out = h_grid ? reinterpret_cast<float*>(st + off_grid) : dl_ddensity;
   float4* dgrid4 = nullptr;
   if (with_density) {
-    // the kernels accumulate into x-quads (vector atomics), folded into the grid afterwards
-    CUDA_TRY(c, c->grad4.ensure(grid_elems * sizeof(float4)));
+    // the kernels accumulate into x-quads (vector atomics), folded into the
+    // grid afterwards; the fold leaves the buffer zero for the next call
+    const size_t want = grid_elems * sizeof(float4);
+    if (want > c->grad4.bytes) c->grad4_zero = false;
+    CUDA_TRY(c, c->grad4.ensure(want));
     dgrid4 = static_cast<float4*>(c->grad4.ptr);
-    CUDA_TRY(c, cudaMemsetAsync(dgrid4, 0, grid_elems * sizeof(float4), s));
+    if (!c->grad4_zero) CUDA_TRY(c, cudaMemsetAsync(dgrid4, 0, c->grad4.bytes, s));
+    c->grad4_zero = false;
   }
   for (int i = 0; i < n_views; ++i)
     if (off_dl[i] != SIZE_MAX)
@@ -1544,7 +1552,10 @@ int backward_views(aloha_ctx* c, int n_views, const int* view_ids, const float* 
       CUDA_TRY(c, launch_backward(a, c->num_sms * per_sm, s));
     }
   }
-  if (with_density) CUDA_TRY(c, launch_fold_quads(dgrid4, grid_out, grid_dims, s));
+  if (with_density) {
+    CUDA_TRY(c, launch_fold_quads(dgrid4, grid_out, grid_dims, s));
+    c->grad4_zero = true;
+  }
   c->samples_valid = true;
   if (h_tf) CUDA_TRY(c, cudaMemcpyAsync(dl_dtf, dtf, tf_bytes, cudaMemcpyDeviceToHost, s));
   if (h_grid) CUDA_TRY(c, cudaMemcpyAsync(dl_ddensity, grid_out, g_bytes, cudaMemcpyDeviceToHost, s));

@@ -272,6 +272,42 @@ def test_backward_errors(gpu_ctx_factory):
 
 
 @pytest.mark.parametrize("bricks", [1, 8])
+def test_gradient_buffer_is_clear_between_calls(gpu_ctx_factory, bricks):
+    """The fold leaves the x-quad gradient buffer zero for the next call (no
+    memset between calls): repeated density backwards agree, a larger grid
+    around the bricks holds the same gradient with zeros outside, a smaller
+    grid after it and calls after a failed one agree again."""
+    n = 40
+    vol, descs, vox = density_scene(n, seed=23, bricks=bricks)
+    ctx = setup(gpu_ctx_factory, descs, vox, S.ramp_tf())
+    W, H = 64, 56
+    cam = T.cameras((n, n, n), 1, W, H, seed=5)[0]
+    ctx.set_camera(0, *cam)
+    ctx.resize(0, W, H)
+    ctx.forward(0, np.zeros((H, W, 4), np.float32), 16)
+    dl = np.random.default_rng(3).uniform(-1, 1, (H, W, 4)).astype(np.float32)
+
+    def density(lo=(0, 0, 0), dims=(n, n, n)):
+        g = np.zeros(dims[::-1], np.float32)
+        ctx.backward(0, dl, None, g, lo, dims)
+        return g
+
+    first = density()
+    assert np.count_nonzero(first) > 500
+    tol = dict(rtol=1e-5, atol=1e-6 * float(np.abs(first).max()))
+    np.testing.assert_allclose(density(), first, **tol)
+    big = density((-3, -2, -1), (n + 7, n + 5, n + 2))
+    np.testing.assert_allclose(big[1:1 + n, 2:2 + n, 3:3 + n], first, **tol)
+    inner = np.zeros(big.shape, bool)
+    inner[1:1 + n, 2:2 + n, 3:3 + n] = True
+    assert not big[~inner].any()
+    np.testing.assert_allclose(density(), first, **tol)
+    with pytest.raises(abi.AlohaError):
+        ctx.backward(0, dl, None, np.zeros((n, n, n), np.float32), (0, 0, 0), (n - 1, n, n))
+    np.testing.assert_allclose(density(), first, **tol)
+
+
+@pytest.mark.parametrize("bricks", [1, 8])
 def test_tf_only_backward(gpu_ctx_factory, oracle, bricks):
     """Without a density gradient (dl_ddensity NULL) the backward skips the
     shading and stencil adjoints; its transfer-function gradient must match the
