@@ -319,8 +319,8 @@ int aloha_backward(aloha_ctx* ctx, int view, const float* dl_drgba, float* dl_dt
  * sum over views[0..n_views) of each view's gradient, with dl_drgba[i] the
  * dL/dRGBA of views[i] (each view at most once, each with a current
  * aloha_forward).  Same arguments and rules as aloha_backward otherwise.  The
- * views' replays accumulate into one device buffer that is cleared and folded
- * into the density grid once, their checkpoint-overflow flags are read with
+ * views' replays accumulate into one device buffer that is folded into the
+ * density grid once (the fold leaves it clear for the next call), their checkpoint-overflow flags are read with
  * one host wait, and one persistent launch replays every view's segments, so
  * n views cost less than n calls of aloha_backward.  The views may have been
  * forwarded with different checkpoint intervals.
