@@ -106,9 +106,9 @@ __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevVi
       const float uy = fmaf(t, ray.d[1], ray.o[1]) - b.lo[1];
       const float uz = fmaf(t, ray.d[2], ray.o[2]) - b.lo[2];
       if (SKIP && b.empty && !(t < t_cell)) {
-        const int mx = min(max((int)floorf(ux), 0), b.n[0] - 1) >> kMacroShift;
-        const int my = min(max((int)floorf(uy), 0), b.n[1] - 1) >> kMacroShift;
-        const int mz = min(max((int)floorf(uz), 0), b.n[2] - 1) >> kMacroShift;
+        const int mx = min(max(__float2int_rd(ux), 0), b.n[0] - 1) >> kMacroShift;
+        const int my = min(max(__float2int_rd(uy), 0), b.n[1] - 1) >> kMacroShift;
+        const int mz = min(max(__float2int_rd(uz), 0), b.n[2] - 1) >> kMacroShift;
         const float bnd[3] = {(float)(mx << kMacroShift), (float)(my << kMacroShift), (float)(mz << kMacroShift)};
         float tb = t1;
 #pragma unroll
@@ -133,7 +133,7 @@ __device__ __forceinline__ uint32_t walk_samples(const TrainArgs& a, const DevVi
           continue;
         }
       }
-      const StencilOut s = stencil(b.base, b.sy, b.sz, b.n[0], b.n[1], b.n[2], ux, uy, uz);
+      const StencilOut s = stencil<true>(b.base, b.sy, b.sz, b.n[0], b.n[1], b.n[2], ux, uy, uz);
       const float shade = shade_factor(s, ray);
       const float4 c = tf_lookup(tf_s, a.n_tf, nf, s.value);
       visit(b, t, w, nb, ux, uy, uz, s, shade, c, color);
@@ -326,18 +326,11 @@ __device__ __forceinline__ void scatter2(const TrainArgs& a, const DevBrick& b, 
 // accumulate into the voxel they copy.
 __device__ __forceinline__ void stencil_backward(const DevBrick& b, const TrainArgs& a, int brick, float ux,
                                                  float uy, float uz, float dv, float dgx, float dgy, float dgz) {
-  const float mx = ux - 0.5f, my = uy - 0.5f, mz = uz - 0.5f;
-  const float fmx = floorf(mx), fmy = floorf(my), fmz = floorf(mz);
-  const float fcx = floorf(ux), fcy = floorf(uy), fcz = floorf(uz);
-  const float fx = mx - fmx, fy = my - fmy, fz = mz - fmz;
-  const float gx = ux - fcx, gy = uy - fcy, gz = uz - fcz;
-  const bool hx = fcx != fmx, hy = fcy != fmy, hz = fcz != fmz;
-  const int ix = min(max((int)fmx, -kApron), b.n[0] - 1);
-  const int iy = min(max((int)fmy, -kApron), b.n[1] - 1);
-  const int iz = min(max((int)fmz, -kApron), b.n[2] - 1);
-  const int cx = min(max((int)fcx, -kApron), b.n[0]);
-  const int cy = min(max((int)fcy, -kApron), b.n[1]);
-  const int cz = min(max((int)fcz, -kApron), b.n[2]);
+  // the forward stencil's coordinates (same indices and weights)
+  const AxisCoord X = axis_coord(ux, b.n[0]), Y = axis_coord(uy, b.n[1]), Z = axis_coord(uz, b.n[2]);
+  const float fx = X.f, fy = Y.f, fz = Z.f, gx = X.g, gy = Y.g, gz = Z.g;
+  const bool hx = X.h, hy = Y.h, hz = Z.h;
+  const int ix = X.i, iy = Y.i, iz = Z.i, cx = X.c, cy = Y.c, cz = Z.c;
   const int4 org = a.brick_grid_origin[brick];
   const int ny1 = b.n[1] - 1, nz1 = b.n[2] - 1;
   const float wx[2] = {1.f - gx, gx}, wy[2] = {1.f - gy, gy}, wz[2] = {1.f - gz, gz};
@@ -525,9 +518,8 @@ __device__ __forceinline__ uint32_t backward_item(const TrainArgs& a, const DevV
         const float dA = oma * fmaf(shade, gc, gA);  // dL/d(alpha of this sample)
         // transfer function lookup backward (the lookup of tf_lookup)
         const float xb = s.value * nf - 0.5f;
-        const float fl = floorf(xb);
-        const float wt = xb - fl;
-        const int i0 = (int)fl;
+        const int i0 = __float2int_rd(xb);
+        const float wt = xb - (float)i0;
         const int ic = min(max(i0, -2), a.n_tf);
         const float4 e0 = tf_s[ic + 2], e1 = tf_s[ic + 3];
         if (WITH_TF && i0 != pend_i) {
@@ -580,9 +572,8 @@ __device__ __forceinline__ uint32_t backward_item(const TrainArgs& a, const DevV
     const float dd = e.oma * (gtrue - e.gA);  // change of dL/d(alpha of the sample)
     if (dd == 0.f) continue;
     const float xb = e.value * nf - 0.5f;
-    const float fl = floorf(xb);
-    const float wt = xb - fl;
-    const int i0 = (int)fl;
+    const int i0 = __float2int_rd(xb);
+    const float wt = xb - (float)i0;
     if (WITH_TF) {
       if (i0 >= 0 && i0 < a.n_tf) atomicAdd(dtf_s + i0 * 4 + 3, (1.f - wt) * dd);
       if (i0 + 1 >= 0 && i0 + 1 < a.n_tf) atomicAdd(dtf_s + (i0 + 1) * 4 + 3, wt * dd);

@@ -89,6 +89,52 @@ struct StencilOut {
   float value, gx, gy, gz;
 };
 
+// One axis of the stencil's coordinates at voxel coordinate u: the weight of
+// the centre (g = u - floor u) and of the displaced taps (f = m - floor m,
+// m = u - 1/2), whether floor m = floor u - 1 (h), and the clamped indices
+// i = floor m and c = floor u.  floor u comes from one round-down conversion
+// to an integer k; for |u| < 2^22 (every coordinate of a sample inside a
+// brick) k and k - 1 are exact floats and m = RN(u - 1/2) lies in
+// [k - 1/2, k + 1/2], so floor m = k - (m < k): the same bits as floorf.  For
+// a degenerate coordinate beyond that the indices still clamp into the apron,
+// where every tap along the axis reads the same edge value, so the (finite)
+// weights cannot change the result.
+struct AxisCoord {
+  int i, c;
+  float f, g;
+  bool h;
+};
+
+__device__ __forceinline__ AxisCoord axis_coord(float u, int n) {
+  const float m = u - 0.5f;
+  const int k = __float2int_rd(u);
+  const float fc = (float)k;
+  AxisCoord a;
+  a.h = m < fc;
+  a.f = m - (a.h ? fc - 1.0f : fc);
+  a.g = u - fc;
+  a.c = min(max(k, -kApron), n);
+  a.i = min(max(a.c - (a.h ? 1 : 0), -kApron), n - 1);
+  return a;
+}
+
+// The same coordinates from two float floors per axis (floor u, floor m),
+// each converted to an index.  One more conversion per axis, but the weights
+// do not wait for an integer-to-float conversion: the render's march, bound
+// by the latency of its dependent chain, measured faster this way, the
+// backward (which also scatters) the other way.
+__device__ __forceinline__ AxisCoord axis_coord_floors(float u, int n) {
+  const float m = u - 0.5f;
+  const float fm = floorf(m), fc = floorf(u);
+  AxisCoord a;
+  a.h = fc != fm;
+  a.f = m - fm;
+  a.g = u - fc;
+  a.c = min(max((int)fc, -kApron), n);
+  a.i = min(max((int)fm, -kApron), n - 1);
+  return a;
+}
+
 // The stencil's arithmetic from its eight loaded rows (shared by the direct
 // loads of stencil() and the staged loads of StagedLoads, so both give the
 // same bits).
@@ -138,23 +184,19 @@ __device__ __forceinline__ StencilOut stencil_rows(const float4 r00, const float
   return s;
 }
 
+// ROUND_DOWN picks axis_coord (one conversion per axis) over
+// axis_coord_floors; both give the same bits.
+template <bool ROUND_DOWN = false>
 __device__ __forceinline__ StencilOut stencil(const float4* __restrict__ base, int sy, int sz, int nx, int ny,
                                               int nz, float ux, float uy, float uz) {
-  const float mx = ux - 0.5f, my = uy - 0.5f, mz = uz - 0.5f;
-  const float fmx = floorf(mx), fmy = floorf(my), fmz = floorf(mz);
-  const float fcx = floorf(ux), fcy = floorf(uy), fcz = floorf(uz);
-  const float fx = mx - fmx, fy = my - fmy, fz = mz - fmz;  // weights of the displaced taps
-  const float gx = ux - fcx, gy = uy - fcy, gz = uz - fcz;  // weights of the centre
-  const bool hx = fcx != fmx, hy = fcy != fmy, hz = fcz != fmz;  // floor(u) == floor(u - 1/2) + 1
   // Indices, clamped into the apron.  Every index the oracle clamps to the
   // edge maps to an apron voxel holding that edge value, so these clamps only
   // keep pathological coordinates in bounds and never change a value.
-  const int ix = min(max((int)fmx, -kApron), nx - 1);
-  const int iy = min(max((int)fmy, -kApron), ny - 1);
-  const int iz = min(max((int)fmz, -kApron), nz - 1);
-  const int cx = min(max((int)fcx, -kApron), nx);
-  const int cy = min(max((int)fcy, -kApron), ny);
-  const int cz = min(max((int)fcz, -kApron), nz);
+  const AxisCoord X = ROUND_DOWN ? axis_coord(ux, nx) : axis_coord_floors(ux, nx);
+  const AxisCoord Y = ROUND_DOWN ? axis_coord(uy, ny) : axis_coord_floors(uy, ny);
+  const AxisCoord Z = ROUND_DOWN ? axis_coord(uz, nz) : axis_coord_floors(uz, nz);
+  const int ix = X.i, iy = Y.i, iz = Z.i, cx = X.c, cy = Y.c, cz = Z.c;
+  const bool hx = X.h, hy = Y.h, hz = Z.h;  // floor(u) == floor(u - 1/2) + 1
 
   // X region: x in {ix, ix+1, ix+2}, y in {cy, cy+1}, z in {cz, cz+1}: one
   // quad per (y, z) row.
@@ -168,7 +210,7 @@ __device__ __forceinline__ StencilOut stencil(const float4* __restrict__ base, i
   const float2 e0 = __ldg(reinterpret_cast<const float2*>(p1)), e1 = __ldg(reinterpret_cast<const float2*>(p1 + sz));
   const float4* p2 = base + (ze * sz + cy * sy + cx);
   const float2 f0 = __ldg(reinterpret_cast<const float2*>(p2)), f1 = __ldg(reinterpret_cast<const float2*>(p2 + sy));
-  return stencil_rows(r00, r10, r01, r11, e0, e1, f0, f1, fx, fy, fz, gx, gy, gz, hx, hy, hz);
+  return stencil_rows(r00, r10, r01, r11, e0, e1, f0, f1, X.f, Y.f, Z.f, X.g, Y.g, Z.g, hx, hy, hz);
 }
 
 // ---- Where the stencil's rows come from -----------------------------------
@@ -241,16 +283,10 @@ struct StagedLoads {
   // addresses of stencil(), clamped into the apron.
   __device__ __forceinline__ void issue(int slot, const float4* __restrict__ base, int sy, int sz, int nx, int ny,
                                         int nz, float ux, float uy, float uz) const {
-    const float fmx = floorf(ux - 0.5f), fmy = floorf(uy - 0.5f), fmz = floorf(uz - 0.5f);
-    const float fcx = floorf(ux), fcy = floorf(uy), fcz = floorf(uz);
-    const int ix = min(max((int)fmx, -kApron), nx - 1);
-    const int iy = min(max((int)fmy, -kApron), ny - 1);
-    const int iz = min(max((int)fmz, -kApron), nz - 1);
-    const int cx = min(max((int)fcx, -kApron), nx);
-    const int cy = min(max((int)fcy, -kApron), ny);
-    const int cz = min(max((int)fcz, -kApron), nz);
-    const int ye = fcy != fmy ? iy : iy + 2;
-    const int ze = fcz != fmz ? iz : iz + 2;
+    const AxisCoord X = axis_coord_floors(ux, nx), Y = axis_coord_floors(uy, ny), Z = axis_coord_floors(uz, nz);
+    const int ix = X.i, iy = Y.i, iz = Z.i, cx = X.c, cy = Y.c, cz = Z.c;
+    const int ye = Y.h ? iy : iy + 2;
+    const int ze = Z.h ? iz : iz + 2;
     const float4* p0 = base + (cz * sz + cy * sy + ix);
     const float4* p1 = base + (cz * sz + ye * sy + cx);
     const float4* p2 = base + (ze * sz + cy * sy + cx);
@@ -288,12 +324,10 @@ struct StagedLoads {
     }
     const float4 r00 = *row(cur, 0), r10 = *row(cur, 1), r01 = *row(cur, 2), r11 = *row(cur, 3);
     const float4 ef = *row(cur, 4), ff = *row(cur, 5);
-    const float mx = ux - 0.5f, my = uy - 0.5f, mz = uz - 0.5f;
-    const float fmx = floorf(mx), fmy = floorf(my), fmz = floorf(mz);
-    const float fcx = floorf(ux), fcy = floorf(uy), fcz = floorf(uz);
+    const AxisCoord X = axis_coord_floors(ux, nx), Y = axis_coord_floors(uy, ny), Z = axis_coord_floors(uz, nz);
     const StencilOut s = stencil_rows(r00, r10, r01, r11, make_float2(ef.x, ef.y), make_float2(ef.z, ef.w),
-                                      make_float2(ff.x, ff.y), make_float2(ff.z, ff.w), mx - fmx, my - fmy, mz - fmz,
-                                      ux - fcx, uy - fcy, uz - fcz, fcx != fmx, fcy != fmy, fcz != fmz);
+                                      make_float2(ff.x, ff.y), make_float2(ff.z, ff.w), X.f, Y.f, Z.f, X.g, Y.g,
+                                      Z.g, X.h, Y.h, Z.h);
     t_staged = next ? tn : __int_as_float(0x7fffffff);
     inflight = next;
     cur ^= 1;
@@ -383,9 +417,9 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
       const float uy = fmaf(t, r.d[1], r.o[1]) - loy;
       const float uz = fmaf(t, r.d[2], r.o[2]) - loz;
       if (empty && !(t < t_cell)) {
-        const int mx = min(max((int)floorf(ux), 0), nx - 1) >> kMacroShift;
-        const int my = min(max((int)floorf(uy), 0), ny - 1) >> kMacroShift;
-        const int mz = min(max((int)floorf(uz), 0), nz - 1) >> kMacroShift;
+        const int mx = min(max(__float2int_rd(ux), 0), nx - 1) >> kMacroShift;
+        const int my = min(max(__float2int_rd(uy), 0), ny - 1) >> kMacroShift;
+        const int mz = min(max(__float2int_rd(uz), 0), nz - 1) >> kMacroShift;
         const float bx = (float)(mx << kMacroShift), by = (float)(my << kMacroShift),
                     bz = (float)(mz << kMacroShift);
         const float ex = ((r.d[0] > 0.f ? bx + (float)kMacro - eps : bx + eps) - offx) * idx_;
@@ -426,9 +460,9 @@ __device__ __forceinline__ uint32_t march_brick(const DevBrick& b, const float4*
     const float uy = fmaf(t, r.d[1], r.o[1]) - loy;
     const float uz = fmaf(t, r.d[2], r.o[2]) - loz;
     if (empty && !(t < t_cell)) {
-      const int mx = min(max((int)floorf(ux), 0), nx - 1) >> kMacroShift;
-      const int my = min(max((int)floorf(uy), 0), ny - 1) >> kMacroShift;
-      const int mz = min(max((int)floorf(uz), 0), nz - 1) >> kMacroShift;
+      const int mx = min(max(__float2int_rd(ux), 0), nx - 1) >> kMacroShift;
+      const int my = min(max(__float2int_rd(uy), 0), ny - 1) >> kMacroShift;
+      const int mz = min(max(__float2int_rd(uz), 0), nz - 1) >> kMacroShift;
       // tb: the ray's exit from the macrocell's box shrunk by eps; every
       // sample before it lies in this macrocell.
       const float bx = (float)(mx << kMacroShift), by = (float)(my << kMacroShift), bz = (float)(mz << kMacroShift);
@@ -565,9 +599,9 @@ __device__ __forceinline__ uint32_t march_brick_group(const DevBrick& b, const f
       const float ux = fmaf(t, r.d[0], r.o[0]) - lox;
       const float uy = fmaf(t, r.d[1], r.o[1]) - loy;
       const float uz = fmaf(t, r.d[2], r.o[2]) - loz;
-      const int mx = min(max((int)floorf(ux), 0), nx - 1) >> kMacroShift;
-      const int my = min(max((int)floorf(uy), 0), ny - 1) >> kMacroShift;
-      const int mz = min(max((int)floorf(uz), 0), nz - 1) >> kMacroShift;
+      const int mx = min(max(__float2int_rd(ux), 0), nx - 1) >> kMacroShift;
+      const int my = min(max(__float2int_rd(uy), 0), ny - 1) >> kMacroShift;
+      const int mz = min(max(__float2int_rd(uz), 0), nz - 1) >> kMacroShift;
       const float bx = (float)(mx << kMacroShift), by = (float)(my << kMacroShift), bz = (float)(mz << kMacroShift);
       const float ex = ((r.d[0] > 0.f ? bx + (float)kMacro - eps : bx + eps) - offx) * idx_;
       const float ey = ((r.d[1] > 0.f ? by + (float)kMacro - eps : by + eps) - offy) * idy;
@@ -600,9 +634,9 @@ __device__ __forceinline__ uint32_t march_brick_group(const DevBrick& b, const f
       const float vy = fmaf(tk, r.d[1], r.o[1]) - loy;
       const float vz = fmaf(tk, r.d[2], r.o[2]) - loz;
       if (empty && !(tk < t_cell)) {
-        const int mx = min(max((int)floorf(vx), 0), nx - 1) >> kMacroShift;
-        const int my = min(max((int)floorf(vy), 0), ny - 1) >> kMacroShift;
-        const int mz = min(max((int)floorf(vz), 0), nz - 1) >> kMacroShift;
+        const int mx = min(max(__float2int_rd(vx), 0), nx - 1) >> kMacroShift;
+        const int my = min(max(__float2int_rd(vy), 0), ny - 1) >> kMacroShift;
+        const int mz = min(max(__float2int_rd(vz), 0), nz - 1) >> kMacroShift;
         full = !__ldg(empty + (mz * mny + my) * mnx + mx);
       }
       if (full) {
@@ -667,9 +701,9 @@ template <class Loads = DirectLoads, int G = 1>
 __device__ __forceinline__ float4 march_rank(const FrameArgs& a, const DevView& v, const float4* tf_s, const Ray& ray,
                                              const int* __restrict__ rbricks, int j0, int j1, int pixel, float& z,
                                              uint32_t& ns, Loads& loads, const LaneGroup& g = LaneGroup{0, 0u, 0}) {
-  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
   uint32_t draw = 0;
-  for (int s = 0; s < a.spp; ++s) {
+  // one pass of the rank's bricks (one sample per pixel of spp)
+  auto pass = [&]() -> float4 {
     float4 color = make_float4(0.f, 0.f, 0.f, 0.f);
     float tmin = 0.0f;
     for (int j = j0; j < j1; ++j) {
@@ -687,6 +721,15 @@ __device__ __forceinline__ float4 march_rank(const FrameArgs& a, const DevView& 
       tmin = t1 + 1e-20f;
       if (!(color.w < a.et_alpha)) break;
     }
+    return color;
+  };
+  // The sum over passes starts from the first pass's colour: 0 + c = c, as a
+  // march colour is never -0 (it starts at +0 and every update is an fmaf
+  // onto it, and an exact zero sum rounds to +0).  With one pass no sum is
+  // then live across the march.
+  float4 acc = pass();
+  for (int s = 1; s < a.spp; ++s) {
+    const float4 color = pass();
     acc.x = acc.x + color.x;
     acc.y = acc.y + color.y;
     acc.z = acc.z + color.z;
@@ -742,17 +785,21 @@ __device__ __forceinline__ float4 rank_output(const FrameArgs& a, int W, int H, 
 // Front-to-back ordered "over" of rank images (IceT BLEND with
 // ORDERED_COMPOSITE, waikikiRenderer.cpp:910-917,1042-1079): in fp32, or on
 // images quantised to 8 bits per channel like IceT's RGBA_UBYTE buffers.
+// One float4 holds the state of either mode (the ubyte channels as the bits
+// of its components; all-zero bits are 0.0f and 0u), so the blend keeps four
+// registers live across the march, not eight.
 struct OverBlend {
   float4 comp = make_float4(0.f, 0.f, 0.f, 0.f);
-  uint32_t c8[4] = {0u, 0u, 0u, 0u};
   __device__ __forceinline__ void add(int mode, float4 img) {
     if (mode == ALOHA_COMPOSITE_UBYTE) {
       const uint32_t q0 = quantize8(img.x), q1 = quantize8(img.y), q2 = quantize8(img.z), q3 = quantize8(img.w);
-      const uint32_t f = 255u - c8[3];
-      c8[0] = min(255u, c8[0] + (q0 * f + 127u) / 255u);
-      c8[1] = min(255u, c8[1] + (q1 * f + 127u) / 255u);
-      c8[2] = min(255u, c8[2] + (q2 * f + 127u) / 255u);
-      c8[3] = min(255u, c8[3] + (q3 * f + 127u) / 255u);
+      const uint32_t c0 = __float_as_uint(comp.x), c1 = __float_as_uint(comp.y), c2 = __float_as_uint(comp.z),
+                     c3 = __float_as_uint(comp.w);
+      const uint32_t f = 255u - c3;
+      comp.x = __uint_as_float(min(255u, c0 + (q0 * f + 127u) / 255u));
+      comp.y = __uint_as_float(min(255u, c1 + (q1 * f + 127u) / 255u));
+      comp.z = __uint_as_float(min(255u, c2 + (q2 * f + 127u) / 255u));
+      comp.w = __uint_as_float(min(255u, c3 + (q3 * f + 127u) / 255u));
     } else {
       const float oma = 1.0f - comp.w;
       comp.x = fmaf(oma, img.x, comp.x);
@@ -762,7 +809,9 @@ struct OverBlend {
     }
   }
   __device__ __forceinline__ uint32_t pack(int mode) const {
-    return mode == ALOHA_COMPOSITE_UBYTE ? (c8[0] | (c8[1] << 8) | (c8[2] << 16) | (c8[3] << 24)) : pack_rgba(comp);
+    return mode == ALOHA_COMPOSITE_UBYTE ? (__float_as_uint(comp.x) | (__float_as_uint(comp.y) << 8) |
+                                            (__float_as_uint(comp.z) << 16) | (__float_as_uint(comp.w) << 24))
+                                         : pack_rgba(comp);
   }
 };
 

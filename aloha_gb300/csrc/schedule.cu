@@ -63,9 +63,9 @@ __device__ uint32_t probe_ray(const ChunkOrderArgs& a, const DevView& v, const i
       const int mnx = (b.n[0] + kMacro - 1) >> kMacroShift, mny = (b.n[1] + kMacro - 1) >> kMacroShift;
       for (int i = 0; i < steps; ++i) {
         const float t = fmaf((float)i, stride, t0);
-        const int mx = min(max((int)floorf(fmaf(t, ray.d[0], ray.o[0]) - b.lo[0]), 0), b.n[0] - 1) >> kMacroShift;
-        const int my = min(max((int)floorf(fmaf(t, ray.d[1], ray.o[1]) - b.lo[1]), 0), b.n[1] - 1) >> kMacroShift;
-        const int mz = min(max((int)floorf(fmaf(t, ray.d[2], ray.o[2]) - b.lo[2]), 0), b.n[2] - 1) >> kMacroShift;
+        const int mx = min(max(__float2int_rd(fmaf(t, ray.d[0], ray.o[0]) - b.lo[0]), 0), b.n[0] - 1) >> kMacroShift;
+        const int my = min(max(__float2int_rd(fmaf(t, ray.d[1], ray.o[1]) - b.lo[1]), 0), b.n[1] - 1) >> kMacroShift;
+        const int mz = min(max(__float2int_rd(fmaf(t, ray.d[2], ray.o[2]) - b.lo[2]), 0), b.n[2] - 1) >> kMacroShift;
         c += __ldg(b.empty + (mz * mny + my) * mnx + mx) ? 0u : 1u;
       }
     }
