@@ -782,6 +782,14 @@ __device__ __forceinline__ float4 rank_output(const FrameArgs& a, int W, int H, 
   return img;
 }
 
+// True when renderFrame's output stage leaves a rank image equal to the
+// march's colour: one sample per pixel, no accumulation, heat map, crosshair
+// or rank planes (then img = acc * (1 / 1) * (1 / 1) = acc exactly).
+__device__ __forceinline__ bool plain_output(const FrameArgs& a) {
+  return a.spp == 1 && a.accum_id == 0 && !a.heat_map && !a.crosshair && !(a.accum && a.accumulate) &&
+         !a.rank_images && !a.rank_depth;
+}
+
 // Front-to-back ordered "over" of rank images (IceT BLEND with
 // ORDERED_COMPOSITE, waikikiRenderer.cpp:910-917,1042-1079): in fp32, or on
 // images quantised to 8 bits per channel like IceT's RGBA_UBYTE buffers.
@@ -843,16 +851,32 @@ __device__ __forceinline__ uint32_t render_pixel(const FrameArgs& a, const DevVi
   const Ray ray = generate_ray(v, x, y);
   OverBlend blend;
   uint32_t total = 0;
-  for (int k = 0; k < R; ++k) {
-    const int r = __ldg(order + k);
-    float z = 1.0f;
-    uint32_t ns = 0;
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (in_island)
-      acc = march_rank<Loads, G>(a, v, tf_s, ray, rbricks, __ldg(rstart + r), __ldg(rstart + r + 1), pixel, z, ns,
-                                 loads, g);
-    blend.add(a.composite_mode, rank_output(a, W, H, r, x, y, pixel, npx, acc, ns, z, a.rank_images, a.rank_depth));
-    total += ns;
+  if (plain_output(a)) {
+    // the output stage is the identity (acc * 1 * 1): nothing it needs stays
+    // live across the march
+    for (int k = 0; k < R; ++k) {
+      const int r = __ldg(order + k);
+      float z = 1.0f;
+      uint32_t ns = 0;
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (in_island)
+        acc = march_rank<Loads, G>(a, v, tf_s, ray, rbricks, __ldg(rstart + r), __ldg(rstart + r + 1), pixel, z, ns,
+                                   loads, g);
+      blend.add(a.composite_mode, acc);
+      total += ns;
+    }
+  } else {
+    for (int k = 0; k < R; ++k) {
+      const int r = __ldg(order + k);
+      float z = 1.0f;
+      uint32_t ns = 0;
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (in_island)
+        acc = march_rank<Loads, G>(a, v, tf_s, ray, rbricks, __ldg(rstart + r), __ldg(rstart + r + 1), pixel, z, ns,
+                                   loads, g);
+      blend.add(a.composite_mode, rank_output(a, W, H, r, x, y, pixel, npx, acc, ns, z, a.rank_images, a.rank_depth));
+      total += ns;
+    }
   }
   if (fb_out && (G == 1 || g.lane == 0)) fb_out[fb_index] = blend.pack(a.composite_mode);
   return total;
