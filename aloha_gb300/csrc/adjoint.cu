@@ -255,7 +255,8 @@ __device__ __forceinline__ void forward_item(const TrainArgs& a, unsigned item, 
 // Persistent training forward over the launch's views: warps pull items
 // (a view's 8 x 4 chunk, in its cost order when it has one, else
 // centre-out, as the render does) from the launch's counter.
-__global__ void __launch_bounds__(128, kSingleRenderBlocks) forward_train_kernel(TrainArgs a, unsigned items) {
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) forward_train_kernel(TrainArgs a, unsigned items) {
   extern __shared__ float4 tf_s[];
   load_tf(tf_s, a.tf, a.n_tf);
   __syncthreads();
@@ -670,17 +671,22 @@ size_t backward_smem(int n_tf, bool with_tf) {
 
 }  // namespace
 
-cudaError_t launch_forward_train(const TrainArgs& a, unsigned items, int max_grid, cudaStream_t s) {
+cudaError_t launch_forward_train(const TrainArgs& a, unsigned items, int max_grid, bool many, cudaStream_t s) {
   int grid = (int)std::min<unsigned>((items + 3) / 4, (unsigned)max_grid);
   if (grid < 1) grid = 1;
-  forward_train_kernel<<<grid, 128, (size_t)(a.n_tf + 4) * sizeof(float4), s>>>(a, items);
+  const size_t smem = (size_t)(a.n_tf + 4) * sizeof(float4);
+  if (many)
+    forward_train_kernel<kTrainForwardBlocksMany><<<grid, 128, smem, s>>>(a, items);
+  else
+    forward_train_kernel<kTrainForwardBlocks><<<grid, 128, smem, s>>>(a, items);
   return cudaGetLastError();
 }
 
-int forward_train_blocks_per_sm(int n_tf) {
+int forward_train_blocks_per_sm(int n_tf, bool many) {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, forward_train_kernel, 128,
-                                                    (size_t)(n_tf + 4) * sizeof(float4)) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &n, many ? forward_train_kernel<kTrainForwardBlocksMany> : forward_train_kernel<kTrainForwardBlocks>, 128,
+          (size_t)(n_tf + 4) * sizeof(float4)) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }

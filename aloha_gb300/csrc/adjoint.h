@@ -78,8 +78,10 @@ struct TrainArgs {
 };
 
 // One persistent training forward over the launch's views (a.tv, a.runs).
-cudaError_t launch_forward_train(const TrainArgs& a, unsigned items, int max_grid, cudaStream_t s);
-int forward_train_blocks_per_sm(int n_tf);
+// `many` selects the instance for launches of many chunks per resident warp
+// (kTrainForwardBlocksMany CTAs per SM instead of kTrainForwardBlocks).
+cudaError_t launch_forward_train(const TrainArgs& a, unsigned items, int max_grid, bool many, cudaStream_t s);
+int forward_train_blocks_per_sm(int n_tf, bool many);
 // One persistent backward over the launch's views' items (a.tv, a.item_base).
 cudaError_t launch_backward(const TrainArgs& a, int grid, cudaStream_t s);
 // out[v] += quads[v].x + quads[v-1].y + quads[v-2].z along x, for a grid of

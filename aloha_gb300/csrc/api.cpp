@@ -1383,9 +1383,14 @@ int forward_views(aloha_ctx* c, int n_views, const int* view_ids, float* const* 
   a.n_runs = n_runs;
   a.run_views = reinterpret_cast<const int*>(dev[3]);
   CUDA_TRY(c, cudaMemsetAsync(c->counter.ptr, 0, sizeof(unsigned long long), s));
-  const int per_sm = forward_train_blocks_per_sm(c->n_tf);
+  // few chunks per resident warp: the launch ends on its longest rays (fewer,
+  // faster warps); many: throughput-bound (more warps)
+  const int few_per_sm = forward_train_blocks_per_sm(c->n_tf, false);
+  if (few_per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "forward occupancy query failed");
+  const bool many = items >= (unsigned long long)kTrainManyChunksPerWarp * few_per_sm * c->num_sms * 4;
+  const int per_sm = many ? forward_train_blocks_per_sm(c->n_tf, true) : few_per_sm;
   if (per_sm <= 0) return c->fail(ALOHA_ERR_CUDA, "forward occupancy query failed");
-  CUDA_TRY(c, launch_forward_train(a, (unsigned)items, per_sm * c->num_sms, s));
+  CUDA_TRY(c, launch_forward_train(a, (unsigned)items, per_sm * c->num_sms, many, s));
   c->samples_valid = true;
   bool any_host = false;
   for (int i = 0; i < n_views; ++i) {

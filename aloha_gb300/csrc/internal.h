@@ -159,6 +159,12 @@ cudaError_t launch_pad_brick(const float* src, int nx, int ny, int nz, float4* d
                              int* nonfinite_flag, cudaStream_t s);
 // Persistent render launch; `batch` selects the instance tuned for batches.
 constexpr int kSingleRenderBlocks = 5, kBatchRenderBlocks = 7;  // CTAs per SM
+// CTAs per SM of the differentiable form's forward (checkpointed march): a
+// launch of few chunks ends on its longest rays and runs faster with fewer,
+// faster warps; one of at least kTrainManyChunksPerWarp chunks per resident
+// warp is throughput-bound and runs faster with more.
+constexpr int kTrainForwardBlocks = 5, kTrainForwardBlocksMany = 7;
+constexpr int kTrainManyChunksPerWarp = 16;
 // `stage`: ALOHA_STAGING_NONE or _NEXT_SAMPLE (the stencil loads), or, for
 // batches, kStageUnroll2: direct loads with the march loop written out two
 // steps per trip.

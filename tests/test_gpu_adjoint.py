@@ -453,6 +453,44 @@ def test_forward_views_equals_single_forwards(gpu_ctx_factory, oracle, bricks):
     assert e.value.code == abi.ERR_INVALID_ARGUMENT
 
 
+def test_many_chunk_training_forward(gpu_ctx_factory):
+    """A training forward of many chunks per resident warp runs the instance
+    with more CTAs per SM: two 1024x800 views forwarded together (51 200
+    chunks) give the same images as each view forwarded alone (25 600 chunks,
+    the other instance), and the same gradients afterwards."""
+    torch = pytest.importorskip("torch")
+    n = 32
+    vol, descs, vox = density_scene(n, seed=29, bricks=8)
+    tf = S.ramp_tf()
+    ctx = setup(gpu_ctx_factory, descs, vox, tf)
+    W, H = 1024, 800
+    cams = T.cameras((n, n, n), 2, W, H, seed=67)
+    for v in range(2):
+        ctx.set_camera(v, *cams[v])
+        ctx.resize(v, W, H)
+    dev = "cuda"
+    alone = [torch.zeros((H, W, 4), device=dev) for _ in range(2)]
+    for v in range(2):
+        ctx.forward(v, alone[v], 16)
+    g = torch.Generator(device=dev).manual_seed(11)
+    dls = [(torch.rand((H, W, 4), generator=g, device=dev) * 2 - 1).contiguous() for _ in range(2)]
+    dtf1 = torch.zeros((256, 4), device=dev)
+    dden1 = torch.zeros((n, n, n), device=dev)
+    ctx.backward_views([0, 1], dls, dtf1, dden1, (0, 0, 0), (n, n, n))
+    together = [torch.zeros((H, W, 4), device=dev) for _ in range(2)]
+    ctx.forward_views([0, 1], together, 16)
+    dtf2 = torch.zeros_like(dtf1)
+    dden2 = torch.zeros_like(dden1)
+    ctx.backward_views([0, 1], dls, dtf2, dden2, (0, 0, 0), (n, n, n))
+    torch.cuda.synchronize()
+    for v in range(2):
+        assert float((alone[v][..., 3] > 0).float().mean()) > 0.05
+        assert torch.equal(together[v], alone[v])
+    for a, b in ((dtf2, dtf1), (dden2, dden1)):
+        assert float(b.abs().max()) > 0
+        torch.testing.assert_close(a, b, rtol=1e-4, atol=1e-5 * float(b.abs().max()))
+
+
 def test_autograd_gradient_flags_and_uploads(gpu_ctx_factory):
     """The binding computes only the gradients autograd asks for, and uploads
     the bricks again only when the density tensor changed."""
