@@ -783,11 +783,14 @@ __device__ __forceinline__ float4 rank_output(const FrameArgs& a, int W, int H, 
 }
 
 // True when renderFrame's output stage leaves a rank image equal to the
-// march's colour: one sample per pixel, no accumulation, heat map, crosshair
-// or rank planes (then img = acc * (1 / 1) * (1 / 1) = acc exactly).
+// march's colour: one sample per pixel, no accumulation, heat map or
+// crosshair (then img = acc * (1 / 1) * (1 / 1) = acc exactly); plain_output
+// also wants no rank planes.
+__device__ __forceinline__ bool plain_output_stage(const FrameArgs& a) {
+  return a.spp == 1 && a.accum_id == 0 && !a.heat_map && !a.crosshair && !(a.accum && a.accumulate);
+}
 __device__ __forceinline__ bool plain_output(const FrameArgs& a) {
-  return a.spp == 1 && a.accum_id == 0 && !a.heat_map && !a.crosshair && !(a.accum && a.accumulate) &&
-         !a.rank_images && !a.rank_depth;
+  return plain_output_stage(a) && !a.rank_images && !a.rank_depth;
 }
 
 // Front-to-back ordered "over" of rank images (IceT BLEND with

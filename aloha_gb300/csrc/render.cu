@@ -294,10 +294,20 @@ __global__ void __launch_bounds__(kRenderThreads, MINB) render_split_kernel(Spli
         uint32_t ns = 0;
         float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
         DirectLoads direct;
-        if (pixel_in_island(s.f, W, x, y))
-          acc = march_rank(s.f, v, tf_s, generate_ray(v, x, y), rbricks, __ldg(rstart + r), __ldg(rstart + r + 1),
-                           pixel, z, ns, direct);
-        rank_output(s.f, W, H, r, x, y, pixel, npx, acc, ns, z, planes, nullptr);
+        const bool in_island = pixel_in_island(s.f, W, x, y);
+        if (plain_output_stage(s.f)) {
+          // the output stage is the identity: only the plane store is left,
+          // so nothing else it needs stays live across the march
+          if (in_island)
+            acc = march_rank(s.f, v, tf_s, generate_ray(v, x, y), rbricks, __ldg(rstart + r), __ldg(rstart + r + 1),
+                             pixel, z, ns, direct);
+          planes[(size_t)r * npx + pixel] = acc;
+        } else {
+          if (in_island)
+            acc = march_rank(s.f, v, tf_s, generate_ray(v, x, y), rbricks, __ldg(rstart + r), __ldg(rstart + r + 1),
+                             pixel, z, ns, direct);
+          rank_output(s.f, W, H, r, x, y, pixel, npx, acc, ns, z, planes, nullptr);
+        }
         n += ns;
       }
       __threadfence();
