@@ -11,11 +11,11 @@ namespace aloha {
 // Padded brick storage: every brick is stored with an apron of kApron voxels
 // on each side, filled with the clamped edge values (cudaAddressModeClamp of
 // waikikiRenderer.cpp:753-755), so the march loop needs no per-tap clamps.
-// Each stored element is an x-quad: the float4 (V(x), V(x+1), V(x+2), V(x+3))
-// (indices clamped), so one 16-byte load fetches the three x columns a
-// stencil row needs.  The march is bound by L1 wavefronts (one per distinct
-// 128-byte line a warp load touches); quads cut the loads per sample from 20
-// to 8 at four times the HBM footprint.
+// Each stored element is a yz-quad: the float4 (V(x,y,z), V(x,y+1,z),
+// V(x,y,z+1), V(x,y+1,z+1)) (indices clamped), so one 16-byte load fetches a
+// voxel's 2x2 (y, z) neighbourhood.  The march is bound by L1 wavefronts (one
+// per distinct 128-byte line a warp load touches); quads cut the loads per
+// sample from 20 to 7 at four times the HBM footprint.
 constexpr int kApron = 2;
 constexpr int kMaxViews = 4096;
 constexpr int kMaxTF = 2048;  // (n + 4) float4 entries stay under 48 KB of shared memory
@@ -27,7 +27,7 @@ constexpr int kMacro = 1 << kMacroShift;
 
 // One brick as the kernels see it (72 bytes).
 struct DevBrick {
-  const float4* base;    // x-quad of voxel (0,0,0) of the voxel range inside the padded array
+  const float4* base;    // yz-quad of voxel (0,0,0) of the voxel range inside the padded array
   const uint8_t* empty;  // [mz][my][mx] 1 = every sample there has alpha 0 (null: no skipping)
   int sy, sz;            // padded row and slice pitch, in quads
   int n[3];              // voxel range size

@@ -10,9 +10,10 @@
 // tap is the trilinear interpolation at u, the six gradient taps sit at
 // u +- 1/2 (the reference's tc +- 0.5/N, deviceCode.cpp:278-284).  u - 1/2 and
 // u + 1/2 differ by exactly 1, so all seven taps read one 20-voxel cross
-// around the cell and share their fractional weights.  With the x-quad brick
-// layout the cross is 4 16-byte and 4 8-byte loads per sample (56 texel
-// fetches in the reference).
+// around the cell and share their fractional weights.  With the yz-quad brick
+// layout (each element holds a voxel's 2x2 (y, z) neighbourhood) the cross is
+// five 16-byte and two 8-byte loads per sample (56 texel fetches in the
+// reference).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -184,6 +185,20 @@ __device__ __forceinline__ StencilOut stencil_rows(const float4 r00, const float
   return s;
 }
 
+// The stencil from its seven loaded yz-quads (element (x,y,z) holds V(x,y,z),
+// V(x,y+1,z), V(x,y,z+1), V(x,y+1,z+1)): q0..q2 at x = ix..ix+2 of row (cy,
+// cz); e0, e1 at x = cx, cx+1 of row (ye, cz); the first halves f0, f1 at
+// x = cx, cx+1 of row (cy, ze).  Regrouped into the x rows stencil_rows takes.
+__device__ __forceinline__ StencilOut stencil_quads(const float4 q0, const float4 q1, const float4 q2,
+                                                    const float4 e0, const float4 e1, const float2 f0,
+                                                    const float2 f1, float fx, float fy, float fz, float gx, float gy,
+                                                    float gz, bool hx, bool hy, bool hz) {
+  return stencil_rows(make_float4(q0.x, q1.x, q2.x, 0.f), make_float4(q0.y, q1.y, q2.y, 0.f),
+                      make_float4(q0.z, q1.z, q2.z, 0.f), make_float4(q0.w, q1.w, q2.w, 0.f), make_float2(e0.x, e1.x),
+                      make_float2(e0.z, e1.z), make_float2(f0.x, f1.x), make_float2(f0.y, f1.y), fx, fy, fz, gx, gy,
+                      gz, hx, hy, hz);
+}
+
 // ROUND_DOWN picks axis_coord (one conversion per axis) over
 // axis_coord_floors; both give the same bits.
 template <bool ROUND_DOWN = false>
@@ -199,18 +214,19 @@ __device__ __forceinline__ StencilOut stencil(const float4* __restrict__ base, i
   const bool hx = X.h, hy = Y.h, hz = Z.h;  // floor(u) == floor(u - 1/2) + 1
 
   // X region: x in {ix, ix+1, ix+2}, y in {cy, cy+1}, z in {cz, cz+1}: one
-  // quad per (y, z) row.
+  // yz-quad per x.
   const float4* p0 = base + (cz * sz + cy * sy + ix);
-  const float4 r00 = __ldg(p0), r10 = __ldg(p0 + sy), r01 = __ldg(p0 + sz), r11 = __ldg(p0 + sz + sy);
-  // Extra y row (iy or iy+2) and extra z slice (iz or iz+2) at x in {cx, cx+1}:
-  // the first half of a quad.
+  const float4 q0 = __ldg(p0), q1 = __ldg(p0 + 1), q2 = __ldg(p0 + 2);
+  // Extra y row (iy or iy+2) at z in {cz, cz+1} and extra z slice (iz or
+  // iz+2) at y in {cy, cy+1}, both at x in {cx, cx+1}: two components of a
+  // yz-quad each.
   const int ye = hy ? iy : iy + 2;
   const int ze = hz ? iz : iz + 2;
   const float4* p1 = base + (cz * sz + ye * sy + cx);
-  const float2 e0 = __ldg(reinterpret_cast<const float2*>(p1)), e1 = __ldg(reinterpret_cast<const float2*>(p1 + sz));
-  const float4* p2 = base + (ze * sz + cy * sy + cx);
-  const float2 f0 = __ldg(reinterpret_cast<const float2*>(p2)), f1 = __ldg(reinterpret_cast<const float2*>(p2 + sy));
-  return stencil_rows(r00, r10, r01, r11, e0, e1, f0, f1, X.f, Y.f, Z.f, X.g, Y.g, Z.g, hx, hy, hz);
+  const float4 e0 = __ldg(p1), e1 = __ldg(p1 + 1);
+  const float4* p2 = base + (ze * sz + cy * sy + cx);  // only (y, y+1) at z: the quads' first halves
+  const float2 f0 = __ldg(reinterpret_cast<const float2*>(p2)), f1 = __ldg(reinterpret_cast<const float2*>(p2 + 1));
+  return stencil_quads(q0, q1, q2, e0, e1, f0, f1, X.f, Y.f, Z.f, X.g, Y.g, Z.g, hx, hy, hz);
 }
 
 // ---- Where the stencil's rows come from -----------------------------------
@@ -241,21 +257,16 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(a), "l"(gmem) : "memory");
 }
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(a), "l"(gmem) : "memory");
-}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N> __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// Shared memory of the staged loads: [2 slots][6 rows][kRenderThreads] float4
+// Shared memory of the staged loads: [2 slots][7 rows][kRenderThreads] float4
 // (each thread's rows strided by the CTA size, so a warp's row reads are
-// contiguous); rows 0-3 are the x-region quads, row 4 the extra y row's two
-// halves, row 5 the extra z slice's.
-constexpr int kStageRows = 6;
+// contiguous): the seven yz-quads of stencil(), in its order.
+constexpr int kStageRows = 7;
 constexpr size_t kStageBytes = (size_t)2 * kStageRows * kRenderThreads * sizeof(float4);
 
 struct StagedLoads {
@@ -291,15 +302,12 @@ struct StagedLoads {
     const float4* p1 = base + (cz * sz + ye * sy + cx);
     const float4* p2 = base + (ze * sz + cy * sy + cx);
     cp_async16(row(slot, 0), p0);
-    cp_async16(row(slot, 1), p0 + sy);
-    cp_async16(row(slot, 2), p0 + sz);
-    cp_async16(row(slot, 3), p0 + sz + sy);
-    float2* e = reinterpret_cast<float2*>(row(slot, 4));
-    float2* f = reinterpret_cast<float2*>(row(slot, 5));
-    cp_async8(e, p1);
-    cp_async8(e + 1, p1 + sz);
-    cp_async8(f, p2);
-    cp_async8(f + 1, p2 + sy);
+    cp_async16(row(slot, 1), p0 + 1);
+    cp_async16(row(slot, 2), p0 + 2);
+    cp_async16(row(slot, 3), p1);
+    cp_async16(row(slot, 4), p1 + 1);
+    cp_async16(row(slot, 5), p2);
+    cp_async16(row(slot, 6), p2 + 1);
     cp_async_commit();
   }
 
@@ -322,12 +330,11 @@ struct StagedLoads {
     } else {
       cp_async_wait<0>();
     }
-    const float4 r00 = *row(cur, 0), r10 = *row(cur, 1), r01 = *row(cur, 2), r11 = *row(cur, 3);
-    const float4 ef = *row(cur, 4), ff = *row(cur, 5);
     const AxisCoord X = axis_coord_floors(ux, nx), Y = axis_coord_floors(uy, ny), Z = axis_coord_floors(uz, nz);
-    const StencilOut s = stencil_rows(r00, r10, r01, r11, make_float2(ef.x, ef.y), make_float2(ef.z, ef.w),
-                                      make_float2(ff.x, ff.y), make_float2(ff.z, ff.w), X.f, Y.f, Z.f, X.g, Y.g,
-                                      Z.g, X.h, Y.h, Z.h);
+    const float4 f0 = *row(cur, 5), f1 = *row(cur, 6);
+    const StencilOut s = stencil_quads(*row(cur, 0), *row(cur, 1), *row(cur, 2), *row(cur, 3), *row(cur, 4),
+                                       make_float2(f0.x, f0.y), make_float2(f1.x, f1.y), X.f, Y.f, Z.f, X.g, Y.g, Z.g,
+                                       X.h, Y.h, Z.h);
     t_staged = next ? tn : __int_as_float(0x7fffffff);
     inflight = next;
     cur ^= 1;

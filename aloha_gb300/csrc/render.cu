@@ -361,27 +361,30 @@ __global__ void composite_u8_kernel(const uint32_t* __restrict__ imgs, const int
   }
 }
 
-// Copies a brick (x fastest) into its padded x-quad array: element (x,y,z)
-// holds V(x..x+3) with every index clamped to the brick (the apron and the
-// quad tails repeat edge values), and flags non-finite voxels.  CTAs take
-// padded rows (y, z), their threads the row's elements, so the index
-// arithmetic is one division per row.
+// Copies a brick (x fastest) into its padded yz-quad array: element (x,y,z)
+// holds V(x,y,z), V(x,y+1,z), V(x,y,z+1), V(x,y+1,z+1) with every index
+// clamped to the brick (the apron and the quads' far rows and slices repeat
+// edge values), and flags non-finite voxels.  CTAs take padded rows (y, z),
+// their threads the row's elements, so the index arithmetic is one division
+// per row; a row reads four source rows, each coalesced along x.
 __global__ void pad_brick_kernel(const float* __restrict__ src, int nx, int ny, int nz, float4* __restrict__ dst,
                                  int px, int py, int pz, int* nonfinite) {
   const int rows = py * pz;
   bool bad = false;
   for (int r = blockIdx.x; r < rows; r += gridDim.x) {
     const int y = r % py, z = r / py;
-    const int sy = min(max(y - kApron, 0), ny - 1);
-    const int sz = min(max(z - kApron, 0), nz - 1);
-    const float* __restrict__ row = src + ((size_t)sz * ny + sy) * nx;
+    const int y0 = min(max(y - kApron, 0), ny - 1), y1 = min(max(y + 1 - kApron, 0), ny - 1);
+    const int z0 = min(max(z - kApron, 0), nz - 1), z1 = min(max(z + 1 - kApron, 0), nz - 1);
+    const float* __restrict__ r00 = src + ((size_t)z0 * ny + y0) * nx;
+    const float* __restrict__ r10 = src + ((size_t)z0 * ny + y1) * nx;
+    const float* __restrict__ r01 = src + ((size_t)z1 * ny + y0) * nx;
+    const float* __restrict__ r11 = src + ((size_t)z1 * ny + y1) * nx;
     float4* __restrict__ out = dst + (size_t)r * px;
     for (int x = threadIdx.x; x < px; x += blockDim.x) {
-      float v[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) v[k] = __ldg(row + min(max(x - kApron + k, 0), nx - 1));
-      bad |= !isfinite(v[0]) || !isfinite(v[1]) || !isfinite(v[2]) || !isfinite(v[3]);
-      out[x] = make_float4(v[0], v[1], v[2], v[3]);
+      const int sx = min(max(x - kApron, 0), nx - 1);
+      const float4 v = make_float4(__ldg(r00 + sx), __ldg(r10 + sx), __ldg(r01 + sx), __ldg(r11 + sx));
+      bad |= !isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z) || !isfinite(v.w);
+      out[x] = v;
     }
   }
   if (bad) atomicOr(nonfinite, 1);
@@ -390,9 +393,9 @@ __global__ void pad_brick_kernel(const float* __restrict__ src, int nx, int ny, 
 // Value range each macrocell's samples can read: a sample whose value-tap
 // cell is c (c = clamp(floor(u), 0, n-1)) reads voxels c and c+1 (clamped), so
 // macrocell m covers voxels [m*kMacro, m*kMacro + kMacro] per axis.  One warp
-// per macrocell: its lanes split the macrocell's (y, z) rows, read each row
-// as x-quads (four voxels per load, the components inside the range used),
-// and combine their minima and maxima with shuffles.
+// per macrocell: its lanes split the macrocell's pairs of (y, z) rows, read
+// each pair as yz-quads (four voxels per load, the components inside the
+// range used), and combine their minima and maxima with shuffles.
 __global__ void macrocell_range_kernel(const float4* __restrict__ base, int sy, int sz, int nx, int ny, int nz,
                                        int mnx, int mny, int mnz, float2* __restrict__ out) {
   const int total = mnx * mny * mnz;
@@ -402,23 +405,25 @@ __global__ void macrocell_range_kernel(const float4* __restrict__ base, int sy, 
     const int mx = i % mnx, my = (i / mnx) % mny, mz = i / (mnx * mny);
     const int x0 = mx * kMacro, y0 = my * kMacro, z0 = mz * kMacro;
     const int x1 = min(x0 + kMacro, nx - 1), y1 = min(y0 + kMacro, ny - 1), z1 = min(z0 + kMacro, nz - 1);
-    const int rows_y = y1 - y0 + 1, rows = rows_y * (z1 - z0 + 1);
+    const int pairs_y = (y1 - y0 + 2) >> 1, pairs = pairs_y * ((z1 - z0 + 2) >> 1);
     float lo = __int_as_float(0x7f800000), hi = -lo;
-    for (int r = lane; r < rows; r += 32) {
-      const float4* row = base + (size_t)(z0 + r / rows_y) * sz + (size_t)(y0 + r % rows_y) * sy;
-      for (int x = x0; x <= x1; x += 4) {
+    for (int r = lane; r < pairs; r += 32) {
+      const int y = y0 + 2 * (r % pairs_y), z = z0 + 2 * (r / pairs_y);
+      const bool y_in = y + 1 <= y1, z_in = z + 1 <= z1;  // the quad's second row / slice inside the range
+      const float4* row = base + (size_t)z * sz + (size_t)y * sy;
+      for (int x = x0; x <= x1; ++x) {
         const float4 q = __ldg(row + x);
         lo = fminf(lo, q.x);
         hi = fmaxf(hi, q.x);
-        if (x + 1 <= x1) {
+        if (y_in) {
           lo = fminf(lo, q.y);
           hi = fmaxf(hi, q.y);
         }
-        if (x + 2 <= x1) {
+        if (z_in) {
           lo = fminf(lo, q.z);
           hi = fmaxf(hi, q.z);
         }
-        if (x + 3 <= x1) {
+        if (y_in && z_in) {
           lo = fminf(lo, q.w);
           hi = fmaxf(hi, q.w);
         }
