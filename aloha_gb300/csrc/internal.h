@@ -13,9 +13,10 @@ namespace aloha {
 // waikikiRenderer.cpp:753-755), so the march loop needs no per-tap clamps.
 // Each stored element is a yz-quad: the float4 (V(x,y,z), V(x,y+1,z),
 // V(x,y,z+1), V(x,y+1,z+1)) (indices clamped), so one 16-byte load fetches a
-// voxel's 2x2 (y, z) neighbourhood.  The march is bound by L1 wavefronts (one
-// per distinct 128-byte line a warp load touches); quads cut the loads per
-// sample from 20 to 7 at four times the HBM footprint.
+// voxel's 2x2 (y, z) neighbourhood and the stencil's core comes from three
+// neighbouring elements of one row (x-quads, V(x..x+3), took the same bytes
+// from four rows and hit L1 less often).  Quads cut the loads per sample from
+// 20 to 7 at four times the HBM footprint.
 constexpr int kApron = 2;
 constexpr int kMaxViews = 4096;
 constexpr int kMaxTF = 2048;  // (n + 4) float4 entries stay under 48 KB of shared memory
