@@ -1435,12 +1435,18 @@ int backward_views(aloha_ctx* c, int n_views, const int* view_ids, const float* 
   if (with_density) {
     for (int a = 0; a < 3; ++a)
       if (grid_dims[a] < 1) return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "grid dims must be positive");
-    grid_elems = (size_t)grid_dims[0] * grid_dims[1] * grid_dims[2];
+    // products below 2^62, so none overflows; the fold takes the grid's (y, z)
+    // rows as an int, and 2^40 voxels are far beyond any device's memory
+    const unsigned long long gx = (unsigned)grid_dims[0], gy = (unsigned)grid_dims[1], gz = (unsigned)grid_dims[2];
+    if (gy * gz > 0x7fffffffull || gx * (gy * gz) > (1ull << 40))
+      return c->fail(ALOHA_ERR_OUT_OF_RANGE, "a gradient grid of %d x %d x %d voxels is too large", grid_dims[0],
+                     grid_dims[1], grid_dims[2]);
+    grid_elems = (size_t)(gx * gy * gz);
   }
   for (size_t b = 0; b < origin.size(); ++b) {
     const aloha_brick_desc& d = c->descs[b];
     for (int a = 0; a < 3; ++a)
-      if (d.voxel_lo[a] < grid_lo[a] || d.voxel_hi[a] > grid_lo[a] + grid_dims[a])
+      if (d.voxel_lo[a] < grid_lo[a] || (long long)d.voxel_hi[a] > (long long)grid_lo[a] + grid_dims[a])
         return c->fail(ALOHA_ERR_OUT_OF_RANGE, "brick %zu's voxel range leaves the gradient grid", b);
     origin[b] = make_int4(d.voxel_lo[0] - grid_lo[0], d.voxel_lo[1] - grid_lo[1], d.voxel_lo[2] - grid_lo[2], 0);
   }

@@ -265,6 +265,15 @@ def test_backward_errors(gpu_ctx_factory):
     with pytest.raises(abi.AlohaError) as e:
         ctx.backward(0, img, dtf, dden, (0, 0, 0), (16, 32, 32))  # grid does not cover the bricks
     assert e.value.code == abi.ERR_OUT_OF_RANGE
+    # grids whose voxel count or row count is out of range are refused before
+    # anything is allocated or launched
+    for dims in ((1 << 21, 1 << 10, 1 << 10), (32, 1 << 16, 1 << 16), (2**31 - 1, 2**31 - 1, 2**31 - 1)):
+        with pytest.raises(abi.AlohaError) as e:
+            ctx.backward(0, img, dtf, dden, (0, 0, 0), dims)
+        assert e.value.code == abi.ERR_OUT_OF_RANGE, dims
+    with pytest.raises(abi.AlohaError) as e:  # grid_lo + grid_dims beyond int range
+        ctx.backward(0, img, dtf, dden, (2**31 - 40, 0, 0), (64, 32, 32))
+    assert e.value.code == abi.ERR_OUT_OF_RANGE
     ctx.set_camera(0, *cam)
     with pytest.raises(abi.AlohaError) as e:
         ctx.backward(0, img, dtf, dden, (0, 0, 0), (32, 32, 32))  # camera changed since the forward
