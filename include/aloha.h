@@ -304,7 +304,9 @@ int aloha_forward_views(aloha_ctx* ctx, int n_views, const int* views, float* co
  * densities, given dL/dRGBA of the last aloha_forward of `view`
  * ([height][width][4] float).  Accumulates (+=) into dl_dtf ([n_tf][4]) and
  * into dl_ddensity, a float grid [dims z][dims y][dims x] whose voxel (0,0,0)
- * is grid_lo; every brick's voxel range must lie inside it.  Ghost voxels and
+ * is grid_lo; every brick's voxel range must lie inside it, and the grid may
+ * hold at most 2^40 voxels in at most 2^31 - 1 (y, z) rows (else
+ * ALOHA_ERR_OUT_OF_RANGE, before anything is allocated).  Ghost voxels and
  * clamped edge taps add into the voxel they copy.  Host or device buffers.
  * dl_dtf may be NULL: only the density gradient is computed, and the replay
  * then skips empty macrocells (their samples have transfer-function alpha 0,
