@@ -818,9 +818,10 @@ int aloha_set_bricks(aloha_ctx* c, const aloha_brick_desc* descs, const float* c
     if (!voxels[b]) return c->fail(ALOHA_ERR_NULL_POINTER, "voxels[%d] is null", b);
     int nsz[3];
     for (int a = 0; a < 3; ++a) {
-      nsz[a] = d.voxel_hi[a] - d.voxel_lo[a];
-      if (nsz[a] <= 0 || nsz[a] > 16384)
-        return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "brick %d: voxel range size %d on axis %d", b, nsz[a], a);
+      const long long size = (long long)d.voxel_hi[a] - d.voxel_lo[a];
+      if (size <= 0 || size > 16384)
+        return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "brick %d: voxel range size %lld on axis %d", b, size, a);
+      nsz[a] = (int)size;
       if (!(std::isfinite(d.space_lo[a]) && std::isfinite(d.space_hi[a]) && d.space_lo[a] < d.space_hi[a]))
         return c->fail(ALOHA_ERR_INVALID_ARGUMENT, "brick %d: empty or non-finite space range", b);
     }
