@@ -1226,7 +1226,9 @@ unsigned checkpoint_capacity(const aloha_ctx* c, unsigned k) {
   double d2 = 0;
   for (int a = 0; a < 3; ++a) d2 += (double)(c->bounds_hi[a] - c->bounds_lo[a]) * (c->bounds_hi[a] - c->bounds_lo[a]);
   const double bound = std::sqrt(d2) / c->params.dt + 2.0 * (double)c->descs.size() + 16.0;
-  return (unsigned)std::ceil(bound / k) + 1;
+  // saturated (a tiny dt): the segment-count check then refuses the view
+  const double per_pixel = std::ceil(bound / k) + 1.0;
+  return per_pixel < 4294967295.0 ? (unsigned)per_pixel : 0xffffffffu;
 }
 
 TrainArgs train_args(aloha_ctx* c) {
