@@ -51,8 +51,9 @@ int configure(aloha_batch* b) {
   for (size_t i = 0; i < b->views.size(); ++i) {
     int w = 0, h = 0;
     ctx_view_size(c, b->views[i], &w, &h);
-    const int tiles = ring_slots(w, h, b->tile_w, b->tile_h);
-    prefix[i + 1] = prefix[i] + tiles;
+    const long long next = (long long)prefix[i] + ring_slots(w, h, b->tile_w, b->tile_h);
+    if (next > 0x7fffffffll) return ctx_fail(c, ALOHA_ERR_UNSUPPORTED, "batch: more than 2^31 - 1 tiles in all views");
+    prefix[i + 1] = (int)next;
   }
   b->total_tiles = prefix.back();
   if (cudaMemcpy(b->d_prefix, prefix.data(), sizeof(int) * prefix.size(), cudaMemcpyHostToDevice) != cudaSuccess)
