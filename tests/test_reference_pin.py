@@ -79,6 +79,23 @@ def test_uneven_bricks_match_reference(n_ranks):
         compare(descs, vox, tf, cam, 96, 96, n_ranks)
 
 
+@pytest.mark.parametrize("seed", [77, 4242])
+def test_seeded_transfer_functions_match_reference(seed):
+    """Other transfer functions (seeded colour knots and alpha ramps) on the
+    8-rank scene: the lookup's interpolation and border behaviour."""
+    vol, descs, vox, _ = T.chopsuey_scene(64, 8, seed=seed % 13 + 1)
+    tf = S.seeded_tf(seed)
+    for cam in T.cameras((64, 64, 64), 2, 96, 96, seed=seed % 17):
+        compare(descs, vox, tf, cam, 96, 96, 8)
+
+
+def test_larger_volume_matches_reference():
+    """128^3 in 8 bricks at 192^2: longer rays and more early termination."""
+    vol, descs, vox, tf = T.chopsuey_scene(128, 8)
+    cam = T.cameras((128, 128, 128), 1, 192, 192, seed=3)[0]
+    compare(descs, vox, tf, cam, 192, 192, 8)
+
+
 def test_progressive_accumulation_matches_reference():
     """spp 2 and accumulation over three frames (renderFrame's accumBuffer)."""
     vol, descs, vox, tf = T.chopsuey_scene(48, 8)
